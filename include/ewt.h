@@ -1,0 +1,187 @@
+/*
+ * ewt.h — C ABI of the GB300 wavelet-tree library (libewt.so).
+ *
+ * This is the drop-in boundary for the hot path of mfranzreb/ECL_wavelet:
+ * wavelet-tree construction, RankSelect support over packed bit arrays, and
+ * batched access / rank / select queries.  Every entry point takes plain
+ * pointers and sizes, returns an int status (EWT_OK or a negative EWT_ERR_*),
+ * and never throws.  The C++ header <ecl_wavelet/tree/wavelet_tree.cuh>
+ * wraps it into the reference's ecl::WaveletTree<T> class and rethrows
+ * std::runtime_error with the reference's messages.
+ *
+ * Reference interfaces replaced (paths inside the ECL_wavelet project):
+ *   ewt_build*         WaveletTree<T>::WaveletTree(data, n, alphabet, gpu)
+ *                        include/ecl_wavelet/tree/wavelet_tree.cuh:576-867
+ *   ewt_free           WaveletTree<T>::~WaveletTree   wavelet_tree.cuh:931-943
+ *   ewt_access         WaveletTree<T>::access         wavelet_tree.cuh:956-1231
+ *   ewt_rank           WaveletTree<T>::rank           wavelet_tree.cuh:1247-1551
+ *   ewt_select         WaveletTree<T>::select         wavelet_tree.cuh:1567-1797
+ *   ewt_*_device       accessKernel / rankKernel / selectKernel launched on
+ *                        device-resident queries      wavelet_tree.cuh:373-544
+ *   ewt_mixed*         no counterpart: one launch answers interleaved access,
+ *                        rank and select queries (batched form)
+ *   ewt_get_info       getAlphabetSize / getNumLevels / isMinAlphabet /
+ *                        getCodesStart               wavelet_tree.cuh:2165-2228
+ *   ewt_export         the device arrays the reference keeps private
+ *                        (BitArray words, RankSelect L1/L2/samples, counts,
+ *                        precomputed node ranks), copied to the host
+ *   ewt_get_device_view  the by-value WaveletTree<T> copy a user kernel
+ *                        receives (copy ctor wavelet_tree.cuh:870-887)
+ *   ewt_rs_*           RankSelect(BitArray&&, gpu)   src/bitarray/rank_select.cu:50-304
+ *                        and BitArray(sizes, init)   src/bitarray/bit_array.cu:40-100
+ */
+#ifndef EWT_H
+#define EWT_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EWT_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define EWT_OK 0
+#define EWT_ERR_INVALID_ARGUMENT (-1) /* null pointer, n == 0, bad elem size */
+#define EWT_ERR_OUT_OF_MEMORY (-2)    /* device or pinned allocation failed  */
+#define EWT_ERR_CUDA (-3)             /* any other CUDA runtime error        */
+#define EWT_ERR_ALPHABET (-4) /* alphabet unsorted, < 2 symbols, or the text
+                                 holds a symbol above the last one          */
+#define EWT_ERR_QUERY (-5)    /* a batch held an invalid query: select with
+                                 k == 0, rank with index > n, or a symbol
+                                 above the alphabet's last symbol; the other
+                                 answers of the batch are still written     */
+#define EWT_ERR_UNSUPPORTED (-6)
+#define EWT_ERR_TIMEOUT (-7) /* a bounded device-side wait gave up        */
+#define EWT_ERR_TOO_LARGE (-8) /* size beyond a stated fixed maximum      */
+
+/* ---- query types of the mixed batch ----------------------------------- */
+#define EWT_Q_ACCESS 0
+#define EWT_Q_RANK 1
+#define EWT_Q_SELECT 2
+
+/* ---- components returned by ewt_export / ewt_rs_export ----------------- */
+#define EWT_EXP_COUNTS 1         /* u64 x sigma: exclusive prefix C[c]       */
+#define EWT_EXP_LEVEL_WORDS 2    /* u32 x ceil(bits/32) of one level/array   */
+#define EWT_EXP_L1 3             /* u64 x num_l1 of one level/array          */
+#define EWT_EXP_L2 4             /* u16 x num_l2 of one level/array          */
+#define EWT_EXP_SAMPLES0 5       /* u64 select samples of zeros              */
+#define EWT_EXP_SAMPLES1 6       /* u64 select samples of ones               */
+#define EWT_EXP_TOTAL_ONES 7     /* u64 x levels (or arrays)                 */
+#define EWT_EXP_LEVEL_SIZES 8    /* u64 x levels (or arrays): bits per array */
+#define EWT_EXP_NODE_RANKS 9     /* u64 x num_ranks: rank0 at node starts    */
+#define EWT_EXP_NODE_INFOS 10    /* (u64 start, u64 level) x num_ranks       */
+#define EWT_EXP_CODES 11         /* (u64 len, u64 code) x num_codes          */
+#define EWT_EXP_NODES_AT_LEVEL 12 /* u64 x levels                            */
+#define EWT_EXP_ALPHABET 13      /* u64 x sigma, sorted                      */
+#define EWT_EXP_NUM_LAST_L2 14   /* u64 x levels (or arrays)                 */
+
+typedef struct ewt_info {
+  uint64_t n;                          /* text length                      */
+  uint64_t sigma;                      /* alphabet size                    */
+  uint64_t num_ranks;                  /* node starts with a stored rank0  */
+  uint64_t codes_start;                /* first symbol with a short code   */
+  uint64_t num_codes;                  /* sigma - codes_start              */
+  uint64_t num_nodes_until_last_level; /* node starts above the last level */
+  uint32_t levels;                     /* ceil(log2(sigma))                */
+  uint32_t elem_size;                  /* bytes per text symbol            */
+  uint32_t is_min_alphabet;            /* alphabet == 0..sigma-1           */
+  uint32_t is_pow2;                    /* sigma is a power of two          */
+  uint64_t device_bytes;               /* device memory held by the index  */
+} ewt_info;
+
+typedef struct ewt_tree ewt_tree; /* opaque built index          */
+typedef struct ewt_rs ewt_rs;     /* opaque standalone RankSelect */
+
+/* ---- construction ------------------------------------------------------
+ * data: n symbols of elem_size bytes (1, 2, 4 or 8), host OR device memory.
+ * alphabet: sorted distinct symbols in host memory (elem_size bytes each), or
+ * NULL with sigma == 0 to detect the alphabet from the text.               */
+int ewt_build(const void* data, uint64_t n, int elem_size,
+              const void* alphabet, uint64_t sigma, int gpu_index,
+              ewt_tree** out);
+int ewt_build_u8(const uint8_t* data, uint64_t n, const uint8_t* alphabet,
+                 uint64_t sigma, uint32_t gpu_index, ewt_tree** out);
+int ewt_build_u16(const uint16_t* data, uint64_t n, const uint16_t* alphabet,
+                  uint64_t sigma, uint32_t gpu_index, ewt_tree** out);
+int ewt_build_u32(const uint32_t* data, uint64_t n, const uint32_t* alphabet,
+                  uint64_t sigma, uint32_t gpu_index, ewt_tree** out);
+int ewt_build_u64(const uint64_t* data, uint64_t n, const uint64_t* alphabet,
+                  uint64_t sigma, uint32_t gpu_index, ewt_tree** out);
+/* Same as ewt_build but asynchronous on `stream` for a device-resident text;
+ * the returned tree is usable on that stream once this returns.           */
+int ewt_build_device_async(const void* d_data, uint64_t n, int elem_size,
+                           const void* alphabet, uint64_t sigma,
+                           int gpu_index, void* stream, ewt_tree** out);
+int ewt_free(ewt_tree* tree);
+int ewt_get_info(const ewt_tree* tree, ewt_info* info);
+int ewt_export(const ewt_tree* tree, int component, int level, void* host_buf,
+               uint64_t cap_bytes, uint64_t* size_bytes);
+
+/* ---- host batch queries (synchronous, host buffers) --------------------
+ * queries: m records laid out as ecl::RankSelectQuery<T> — a uint64 index
+ * (rank: position i; select: k >= 1) at byte 0 and the symbol (elem_size
+ * bytes) at byte 8, 16 bytes per record.  Symbols are in the original
+ * alphabet.  access results are elem_size-byte symbols; an index >= n yields
+ * 0.  select with k > count(symbol) yields n.                             */
+int ewt_access(ewt_tree* tree, const uint64_t* indices, uint64_t m,
+               void* results);
+int ewt_rank(ewt_tree* tree, const void* queries, uint64_t m,
+             uint64_t* results);
+int ewt_select(ewt_tree* tree, const void* queries, uint64_t m,
+               uint64_t* results);
+/* types[i] in {EWT_Q_ACCESS, EWT_Q_RANK, EWT_Q_SELECT}; every result is a
+ * uint64 (access results are the symbol widened to 64 bits).              */
+int ewt_mixed(ewt_tree* tree, const uint8_t* types, const void* queries,
+              uint64_t m, uint64_t* results);
+
+/* ---- device-resident batch queries (asynchronous on `stream`) ----------
+ * Same layouts as above with device pointers.  Invalid-query reports are
+ * collected on the device; ewt_query_status synchronises `stream` and
+ * returns EWT_ERR_QUERY if any batch since the last call held one.        */
+int ewt_access_device(ewt_tree* tree, const uint64_t* d_indices, uint64_t m,
+                      void* d_results, void* stream);
+int ewt_rank_device(ewt_tree* tree, const void* d_queries, uint64_t m,
+                    uint64_t* d_results, void* stream);
+int ewt_select_device(ewt_tree* tree, const void* d_queries, uint64_t m,
+                      uint64_t* d_results, void* stream);
+int ewt_mixed_device(ewt_tree* tree, const uint8_t* d_types,
+                     const void* d_queries, uint64_t m, uint64_t* d_results,
+                     void* stream);
+int ewt_query_status(ewt_tree* tree, void* stream);
+
+/* Copies the by-value device view (ecl::detail::TreeView) that the C++
+ * header's WaveletTree<T> embeds; view_size must equal sizeof(TreeView).   */
+int ewt_get_device_view(const ewt_tree* tree, void* view_out,
+                        uint64_t view_size);
+
+/* ---- standalone RankSelect over caller bit arrays ----------------------
+ * words: for each array in turn, ceil(bits[a]/32) packed words, bit i of an
+ * array in bit i%32 of word i/32; host or device memory.                   */
+int ewt_rs_build(const uint32_t* words, const uint64_t* bits,
+                 uint32_t num_arrays, int gpu_index, ewt_rs** out);
+int ewt_rs_free(ewt_rs* rs);
+int ewt_rs_export(const ewt_rs* rs, int component, int array, void* host_buf,
+                  uint64_t cap_bytes, uint64_t* size_bytes);
+/* Batched binary queries on one array: value 0 or 1; rank counts `value`
+ * bits in [0, pos) with pos <= bits; select returns the position of the
+ * i-th `value` bit (i >= 1) or `bits` if there are fewer.  Host buffers.  */
+int ewt_rs_rank(ewt_rs* rs, int array, int value, const uint64_t* pos,
+                uint64_t m, uint64_t* results);
+int ewt_rs_select(ewt_rs* rs, int array, int value, const uint64_t* i,
+                  uint64_t m, uint64_t* results);
+int ewt_rs_get_device_view(const ewt_rs* rs, void* view_out,
+                           uint64_t view_size);
+
+/* ---- diagnostics ------------------------------------------------------- */
+const char* ewt_last_error(void); /* message of the calling thread's last
+                                     failed call, "" if none              */
+int ewt_abi_version(void);
+/* Number of kernel launches this library issued since load (all threads). */
+uint64_t ewt_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EWT_H */
