@@ -1,0 +1,454 @@
+"""Benchmark of the GB300 wavelet tree on the reference's headline workload.
+
+Workload (one step): build the wavelet tree of a 6 * 2^30-symbol uint8 text,
+iid uniform over sigma = 256 symbols, already resident in HBM — histogram,
+log2(sigma) level bit arrays with stable partition, RankSelect L1/L2 counts
+and select samples, node-start ranks.  value = text GB/s (text bytes / step
+time), the construction-sweep configuration of the reference.  After the
+timed steps the same tree answers 2^26 mixed queries (40 % access, 40 %
+rank, 20 % select, types interleaved at random) in the batched one-launch
+form and in the plain per-type form, device-resident and end to end from
+pinned host memory; the sweep over sigma in {4, 16, 64} is timed once each.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+`--impl reference` times the CPU restatement of the reference's algorithm
+(oracle/, all host cores) on a bounded sample of the same workload.
+Multi-GPU runs are independent replicas (one text per GPU, no exchange).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = ("Mqueries/s (access/rank/select) + build GB/s; batched vs plain, "
+          "bit-exact")
+GIB = 1 << 30
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=6 * GIB)
+    p.add_argument("--sigma", type=int, default=256)
+    p.add_argument("--queries", type=int, default=1 << 26)
+    p.add_argument("--no-sweep", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--cpu-sample", type=int, default=1 << 25)
+    return p.parse_args()
+
+
+def measured_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,"
+         "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(prefix="ewt_clocks_", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
+                    "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_baseline_build(sigma, sample, steps=1):
+    """The oracle's build over a bounded sample, on the host cores."""
+    from oracle import oracle as O
+    O.build_library()
+    rng = np.random.default_rng(99)
+    text = rng.integers(0, sigma, sample, dtype=np.uint64).astype(np.uint8)
+    times = []
+    t = None
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        t = O.OracleTree(text, np.arange(sigma))
+        times.append(time.perf_counter() - t0)
+    return text, t, times
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build_library()
+    cores = int(O.lib().ewto_max_threads())
+    sample = args.cpu_sample
+    rng = np.random.default_rng(99)
+    text = rng.integers(0, args.sigma, sample, dtype=np.uint64).astype(np.uint8)
+    alphabet = np.arange(args.sigma)
+    for _ in range(args.warmup):
+        O.OracleTree(text, alphabet)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.OracleTree(text, alphabet)
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * statistics.mean(times)
+    gbs = sample / (ms / 1e3) / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": gbs,
+        "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic: iid uniform uint8 text, seed 99",
+        "config": {"workload": "wavelet-tree build, uint8 text, sigma=%d "
+                               "(bounded CPU sample of the 6*2^30 config)"
+                               % args.sigma, "n": sample,
+                   "sigma": args.sigma, "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": cores,
+                         "kind": "port",
+                         "sample": "%d uint8 symbols, sigma=%d, full build "
+                                   "by the CPU restatement" % (sample,
+                                                               args.sigma)},
+        "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def make_mixed_queries(torch, tree, n, sigma, m, gen):
+    """Device-resident mixed batch: types 40/40/20, RankSelectQuery records."""
+    dev = "cuda"
+    u = torch.rand(m, device=dev, generator=gen)
+    types = torch.where(u < 0.4, 0, torch.where(u < 0.8, 1, 2)).to(torch.uint8)
+    counts = torch.from_numpy(tree.export("COUNTS").astype(np.int64)).to(dev)
+    occ = torch.diff(torch.cat([counts, torch.tensor([n], device=dev)]))
+    sym = torch.randint(0, sigma, (m,), device=dev, generator=gen)
+    acc_idx = torch.randint(0, n, (m,), device=dev, generator=gen)
+    rank_idx = torch.randint(0, n + 1, (m,), device=dev, generator=gen)
+    k = (torch.rand(m, device=dev, generator=gen, dtype=torch.float64)
+         * occ[sym].to(torch.float64)).to(torch.int64) + 1
+    index = torch.where(types == 0, acc_idx, torch.where(types == 1, rank_idx, k))
+    rec = torch.zeros((m, 2), dtype=torch.int64, device=dev)
+    rec[:, 0] = index
+    rec[:, 1] = sym  # symbol in the low byte(s) of the second word
+    return types, rec
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import ecl_wavelet_gb300 as E
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    E.build()
+    dev = torch.device("cuda", local)
+    n, sigma = args.n, args.sigma
+    gen = torch.Generator(device=dev).manual_seed(1234 + rank)
+    text = torch.randint(0, sigma, (n,), dtype=torch.uint8, device=dev,
+                         generator=gen)
+    alphabet = np.arange(sigma)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        E.WaveletTree(text, alphabet, gpu_index=local).close()
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    E.set_timing(True)
+    E.get_timing(reset=True)
+    launches0 = E.launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    tree = None
+    ev0.record(stream)
+    for s in range(args.steps):
+        if tree is not None:
+            tree.close()
+        tree = E.WaveletTree(text, alphabet, gpu_index=local)
+    ev1.record(stream)
+    barrier()
+    step_ms = ev0.elapsed_time(ev1) / args.steps
+    launches = E.launch_count() - launches0
+    phases = E.get_timing(reset=True)
+    E.set_timing(False)
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([step_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        step_ms = float(t.item())
+    value = world * n / (step_ms / 1e3) / 1e9
+
+    # ---- roofline of the dominant build kernel -----------------------------
+    peak, peak_kind = measured_peaks()
+    build_phases = {k: v for k, v in phases.items() if k not in ("query", "h2d")}
+    dom = max(build_phases, key=lambda k: build_phases[k][0])
+    dom_ms, dom_launches = build_phases[dom]
+    L = int(tree.getNumLevels())
+    per_launch_bytes = {
+        # split: read the level order + write the next one (uint8 symbols)
+        "split": 2.0 * n,
+        # fill: read the level order, write one bit per symbol
+        "fill": n + n / 8.0,
+        # rank/select counts: read one level's bits, write L2 + L1
+        "rs_counts": n / 8.0 + 2.0 * n / 512 + 8.0 * n / 65536,
+        "hist": float(n),
+        "samples": 2.0 * L * n / 512 + 16.0 * L * n / 4096,
+        "node_ranks": 0.0,
+    }
+    achieved = (per_launch_bytes.get(dom, 0.0)
+                / (dom_ms / max(dom_launches, 1) / 1e3) / 1e9)
+    traffic = None
+    prof = os.path.join(REPO, "profiles", "traffic_per_symbol.json")
+    if os.path.exists(prof):
+        try:
+            tp = json.load(open(prof))
+            if dom in tp:
+                traffic = tp[dom] * n
+        except Exception:
+            traffic = None
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved,
+                "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": peak_kind, "traffic": traffic,
+                "algorithmic_bytes_per_launch": per_launch_bytes.get(dom)}
+    compulsory = n + L * n / 8.0 + L * n * (8 / 65536 + 2 / 512 + 16 / 4096)
+    build = {"phases_ms_per_step": {k: v[0] / args.steps for k, v in
+                                    phases.items() if v[1]},
+             "compulsory_GB": compulsory / 1e9,
+             "compulsory_frac_of_peak": (compulsory / (step_ms / 1e3) / 1e9)
+             / peak}
+
+    # ---- queries on the last tree -----------------------------------------
+    queries = {}
+    m = args.queries
+    qgen = torch.Generator(device=dev).manual_seed(77 + rank)
+    types, rec = make_mixed_queries(torch, tree, n, sigma, m, qgen)
+    out = torch.empty(m, dtype=torch.int64, device=dev)
+    sptr = stream.cuda_stream
+
+    def timed(fn, reps=3):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    mixed_ms = timed(lambda: tree.mixed_device(types.data_ptr(), rec.data_ptr(),
+                                               m, out.data_ptr(), sptr))
+    assert tree.query_status(sptr) == 0
+    # plain per-type calls over the same queries
+    sel = {t: torch.nonzero(types == t).squeeze(1) for t in (0, 1, 2)}
+    acc_idx = rec[sel[0], 0].contiguous()
+    rq = rec[sel[1]].contiguous()
+    sq = rec[sel[2]].contiguous()
+    o_acc = torch.empty(acc_idx.numel(), dtype=torch.uint8, device=dev)
+    o_r = torch.empty(rq.shape[0], dtype=torch.int64, device=dev)
+    o_s = torch.empty(sq.shape[0], dtype=torch.int64, device=dev)
+    acc_ms = timed(lambda: tree.access_device(acc_idx.data_ptr(),
+                                              acc_idx.numel(),
+                                              o_acc.data_ptr(), sptr))
+    rank_ms = timed(lambda: tree.rank_device(rq.data_ptr(), rq.shape[0],
+                                             o_r.data_ptr(), sptr))
+    sel_ms = timed(lambda: tree.select_device(sq.data_ptr(), sq.shape[0],
+                                              o_s.data_ptr(), sptr))
+    assert tree.query_status(sptr) == 0
+    plain_ms = acc_ms + rank_ms + sel_ms
+    # end to end through the host API (pinned host buffers, copies inside)
+    h_types = types.cpu().pin_memory().numpy()
+    h_rec = rec.cpu().pin_memory().numpy().view(tree.qdtype).reshape(-1)
+    h_out = torch.empty(m, dtype=torch.int64).pin_memory().numpy().view(
+        np.uint64)
+    import ctypes
+    L_ = E.lib()
+
+    def host_mixed():
+        st = L_.ewt_mixed(tree.handle, h_types.ctypes.data, h_rec.ctypes.data,
+                          m, h_out.ctypes.data)
+        assert st == 0
+
+    e2e_q_ms = timed(host_mixed, reps=2)
+    queries = {
+        "n_queries": m, "mix": "40/40/20 access/rank/select, interleaved",
+        "batched_mixed_Mq_s": m / mixed_ms / 1e3,
+        "plain_per_type_Mq_s": m / plain_ms / 1e3,
+        "batched_over_plain": plain_ms / mixed_ms,
+        "access_Mq_s": acc_idx.numel() / acc_ms / 1e3,
+        "rank_Mq_s": rq.shape[0] / rank_ms / 1e3,
+        "select_Mq_s": sq.shape[0] / sel_ms / 1e3,
+        "e2e_mixed_host_Mq_s": m / e2e_q_ms / 1e3,
+        "ms": {"mixed": mixed_ms, "access": acc_ms, "rank": rank_ms,
+               "select": sel_ms, "e2e_mixed": e2e_q_ms},
+    }
+    del out, o_acc, o_r, o_s, rq, sq, acc_idx, rec, types
+
+    # ---- end-to-end build from pinned host memory --------------------------
+    h_text = torch.empty(n, dtype=torch.uint8).pin_memory()
+    h_text.copy_(text)
+    h_np = h_text.numpy()
+    tree.close()
+    tree = None
+    E.WaveletTree(h_np, alphabet, gpu_index=local).close()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = 2
+    for _ in range(reps):
+        tr = E.WaveletTree(h_np, alphabet, gpu_index=local)
+        ones = tr.export("TOTAL_ONES")  # result read back to the host
+        tr.close()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / reps
+    e2e = {"value": world * n / (e2e_ms / 1e3) / 1e9, "unit": "GB/s",
+           "h2d_bytes_per_step": n, "d2h_bytes_per_step": int(ones.nbytes),
+           "ms_per_step": e2e_ms,
+           "queries_Mq_s": queries["e2e_mixed_host_Mq_s"],
+           "queries_h2d_bytes": m * 17, "queries_d2h_bytes": m * 8}
+    del h_text, h_np
+
+    # ---- sigma sweep -------------------------------------------------------
+    sweep = {}
+    if not args.no_sweep:
+        for s in (4, 16, 64, 256):
+            if s == sigma:
+                sweep[str(s)] = value / world
+                continue
+            t2 = torch.randint(0, s, (n,), dtype=torch.uint8, device=dev,
+                               generator=gen)
+            E.WaveletTree(t2, np.arange(s), gpu_index=local).close()
+            torch.cuda.synchronize()
+            a = time.perf_counter()
+            E.WaveletTree(t2, np.arange(s), gpu_index=local).close()
+            torch.cuda.synchronize()
+            sweep[str(s)] = n / (time.perf_counter() - a) / 1e9
+            del t2
+
+    # ---- CPU baseline (rank 0, N = 1 only) ---------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle import oracle as O
+        sample = args.cpu_sample
+        _, ot, times = cpu_baseline_build(sigma, sample)
+        cores = int(O.lib().ewto_max_threads())
+        cpu = {"value": sample / times[-1] / 1e9, "unit": "GB/s",
+               "cores": cores, "kind": "port",
+               "sample": "%d uint8 symbols, sigma=%d: full build by the CPU "
+                         "restatement (level partition single-threaded, "
+                         "counts and queries on all cores)" % (sample, sigma)}
+        rng = np.random.default_rng(5)
+        qm = 1 << 21
+        ty = rng.integers(0, 3, qm).astype(np.uint8)
+        idx = rng.integers(0, sample, qm).astype(np.uint64)
+        sy = rng.integers(0, sigma, qm).astype(np.uint64)
+        idx[ty == 2] = 1 + (idx[ty == 2] % max(1, sample // sigma // 2))
+        a = time.perf_counter()
+        ot.mixed(ty, idx, sy)
+        cpu["mixed_queries_Mq_s"] = qm / (time.perf_counter() - a) / 1e6
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "GB/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": step_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic: iid uniform uint8 text (torch seed %d), "
+                    "device-resident" % 1234,
+            "config": {"workload": "wavelet-tree build of a 6*2^30-symbol "
+                                   "uint8 text, sigma=%d, + %d mixed queries"
+                                   % (sigma, m),
+                       "n": n, "sigma": sigma,
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (6 GiB text)"},
+            "gpu_launches": launches,
+            "roofline": roofline, "build": build, "queries": queries,
+            "sigma_sweep_GB_s": sweep, "e2e": e2e, "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,194 @@
+// Host-side plumbing shared by the libewt.so translation units: status
+// codes from CUDA errors, the per-thread error message behind
+// ewt_last_error(), a launch counter, and small RAII device buffers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "ewt.h"
+
+namespace ewt {
+
+// Status carried through the host code as an exception so that every C-ABI
+// entry point can convert it into an int exactly once.
+struct Error : std::runtime_error {
+  int status;
+  Error(int st, std::string const& msg) : std::runtime_error(msg), status(st) {}
+};
+
+void set_last_error(std::string const& msg);
+void count_launch(uint64_t k = 1);
+
+inline int status_of(cudaError_t e) {
+  return e == cudaErrorMemoryAllocation ? EWT_ERR_OUT_OF_MEMORY : EWT_ERR_CUDA;
+}
+
+#define EWT_CUDA(expr)                                                      \
+  do {                                                                      \
+    cudaError_t _e = (expr);                                                \
+    if (_e != cudaSuccess) {                                                \
+      (void)cudaGetLastError();                                             \
+      throw ::ewt::Error(::ewt::status_of(_e),                              \
+                         std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+    }                                                                       \
+  } while (0)
+
+// Check a kernel launch and count it.
+#define EWT_LAUNCHED()                                                      \
+  do {                                                                      \
+    ::ewt::count_launch();                                                  \
+    cudaError_t _e = cudaGetLastError();                                    \
+    if (_e != cudaSuccess)                                                  \
+      throw ::ewt::Error(::ewt::status_of(_e),                              \
+                         std::string("kernel launch: ") +                  \
+                             cudaGetErrorString(_e));                       \
+  } while (0)
+
+#define EWT_REQUIRE(cond, st, msg)                                          \
+  do {                                                                      \
+    if (!(cond)) throw ::ewt::Error((st), (msg));                           \
+  } while (0)
+
+// Owning device allocation (cudaMalloc / cudaFree).
+class DevBuf {
+ public:
+  DevBuf() = default;
+  explicit DevBuf(size_t bytes) { alloc(bytes); }
+  DevBuf(DevBuf const&) = delete;
+  DevBuf& operator=(DevBuf const&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p_(o.p_), n_(o.n_) { o.p_ = nullptr; o.n_ = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      reset();
+      p_ = o.p_; n_ = o.n_;
+      o.p_ = nullptr; o.n_ = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { reset(); }
+  void alloc(size_t bytes) {
+    reset();
+    if (bytes == 0) bytes = 16;
+    EWT_CUDA(cudaMalloc(&p_, bytes));
+    n_ = bytes;
+  }
+  void reset() {
+    if (p_) cudaFree(p_);
+    p_ = nullptr;
+    n_ = 0;
+  }
+  template <class T> T* as() const { return static_cast<T*>(p_); }
+  void* get() const { return p_; }
+  size_t bytes() const { return n_; }
+
+ private:
+  void* p_ = nullptr;
+  size_t n_ = 0;
+};
+
+// Owning pinned host allocation.
+class PinnedBuf {
+ public:
+  PinnedBuf() = default;
+  PinnedBuf(PinnedBuf const&) = delete;
+  PinnedBuf& operator=(PinnedBuf const&) = delete;
+  ~PinnedBuf() { reset(); }
+  void ensure(size_t bytes) {
+    if (bytes <= n_) return;
+    reset();
+    EWT_CUDA(cudaHostAlloc(&p_, bytes, cudaHostAllocPortable));
+    n_ = bytes;
+  }
+  void reset() {
+    if (p_) cudaFreeHost(p_);
+    p_ = nullptr;
+    n_ = 0;
+  }
+  template <class T> T* as() const { return static_cast<T*>(p_); }
+  size_t bytes() const { return n_; }
+
+ private:
+  void* p_ = nullptr;
+  size_t n_ = 0;
+};
+
+// Device the calling thread should use; restores the previous one on exit.
+class DeviceGuard {
+ public:
+  explicit DeviceGuard(int dev) {
+    EWT_CUDA(cudaGetDevice(&prev_));
+    if (prev_ != dev) EWT_CUDA(cudaSetDevice(dev));
+  }
+  ~DeviceGuard() { cudaSetDevice(prev_); }
+
+ private:
+  int prev_ = 0;
+};
+
+inline bool is_device_pointer(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+inline int sm_count() {
+  static int cached = -1;
+  if (cached < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    cached = v > 0 ? v : 1;
+  }
+  return cached;
+}
+
+inline uint64_t ceil_div(uint64_t a, uint64_t b) { return (a + b - 1) / b; }
+
+// Event-timed phase on one stream (ewt_set_timing / ewt_get_timing).  When
+// timing is off the guard does nothing.
+bool timing_enabled();
+void add_phase_time(int phase, double ms);
+
+class PhaseTimer {
+ public:
+  PhaseTimer(int phase, cudaStream_t s) : phase_(phase), s_(s) {
+    if (!timing_enabled()) return;
+    if (cudaEventCreate(&a_) != cudaSuccess || cudaEventCreate(&b_) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return;
+    }
+    cudaEventRecord(a_, s_);
+    on_ = true;
+  }
+  PhaseTimer(PhaseTimer const&) = delete;
+  PhaseTimer& operator=(PhaseTimer const&) = delete;
+  ~PhaseTimer() {
+    if (!on_) return;
+    float ms = 0.f;
+    if (cudaEventRecord(b_, s_) == cudaSuccess &&
+        cudaEventSynchronize(b_) == cudaSuccess &&
+        cudaEventElapsedTime(&ms, a_, b_) == cudaSuccess)
+      add_phase_time(phase_, ms);
+    (void)cudaGetLastError();
+    cudaEventDestroy(a_);
+    cudaEventDestroy(b_);
+  }
+
+ private:
+  int phase_;
+  cudaStream_t s_;
+  cudaEvent_t a_ = nullptr, b_ = nullptr;
+  bool on_ = false;
+};
+
+}  // namespace ewt

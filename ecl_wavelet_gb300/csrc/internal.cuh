@@ -1,0 +1,109 @@
+// Host-side objects behind the opaque ewt_tree / ewt_rs handles, and the
+// functions the translation units share.
+#pragma once
+#include <memory>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+#include "ecl_wavelet/detail/device_ops.cuh"
+
+namespace ewt {
+
+using ecl::detail::ArrayMeta;
+using ecl::detail::RSView;
+using ecl::detail::TreeView;
+
+// Device storage of a group of bit arrays with rank/select support, laid out
+// as src/bitarray/bit_array.cu:40-100 and src/bitarray/rank_select.cu:50-304
+// do: arrays padded to 32-word multiples, total word count even.
+struct RSStore {
+  std::vector<ArrayMeta> meta;  // host copy
+  DevBuf words, l1, l2, s0, s1, meta_d;
+  uint64_t total_words = 0, total_l1 = 0, total_l2 = 0;
+  uint64_t total_s0 = 0, total_s1 = 0;
+
+  // Lays out arrays of the given bit lengths and allocates words (zeroed),
+  // L1, L2 and the device meta table.  Samples are allocated by build_rs.
+  void layout(std::vector<uint64_t> const& bits);
+  RSView view() const;
+  uint64_t device_bytes() const {
+    return words.bytes() + l1.bytes() + l2.bytes() + s0.bytes() + s1.bytes() +
+           meta_d.bytes();
+  }
+};
+
+// Builds L2/L1/total counts for arrays [first, last) of `rs` on `stream`
+// (the words must be final), copies totals to the host meta.
+void build_rs_counts(RSStore& rs, uint32_t first, uint32_t last,
+                     cudaStream_t stream);
+// Allocates and fills the select samples of every array (needs counts of
+// all arrays) and uploads the final meta table.
+void build_rs_samples(RSStore& rs, cudaStream_t stream);
+
+struct QueryScratch {
+  DevBuf in, out, types;
+  PinnedBuf h_in, h_out, h_types;
+  size_t in_cap = 0, out_cap = 0, types_cap = 0;
+};
+
+struct CodeH {
+  uint64_t len, code;
+};
+struct NodeInfoH {
+  uint64_t start, level;
+};
+
+}  // namespace ewt
+
+struct ewt_tree {
+  int device = 0;
+  uint32_t elem_size = 1;
+  uint64_t n = 0, sigma = 0;
+  uint32_t L = 0;
+  bool is_min = false, pow2 = false;
+  uint64_t codes_start = 0;
+  uint64_t nodes_until_last = 0;
+  std::vector<uint64_t> alphabet;  // original symbols, widened
+  std::vector<uint64_t> occ, counts;
+  std::vector<ewt::CodeH> codes;
+  std::vector<ewt::NodeInfoH> nodes;
+  std::vector<uint64_t> nodes_at_level, node_base, level_bits;
+  ewt::RSStore rs;
+  ewt::DevBuf counts_d, ranks_d, node_base_d, nodes_at_level_d, code_len_d,
+      code_bits_d, alphabet_d, err_d;
+  ecl::detail::TreeView view{};
+  std::mutex query_mu;  // host batch calls share scratch buffers
+  ewt::QueryScratch scratch;
+  cudaStream_t stream = nullptr;  // library-owned stream for host calls
+  uint64_t device_bytes() const;
+};
+
+struct ewt_rs {
+  int device = 0;
+  ewt::RSStore rs;
+  ewt::DevBuf err_d;
+  std::mutex query_mu;
+  ewt::QueryScratch scratch;
+  cudaStream_t stream = nullptr;
+};
+
+namespace ewt {
+// Host orchestration of one tree build (wt_build.cu).
+void build_tree(ewt_tree& t, const void* data, uint64_t n, int elem_size,
+                const void* alphabet, uint64_t sigma, cudaStream_t stream);
+
+// Query launches on device buffers (queries.cu).
+void launch_access(ewt_tree& t, const uint64_t* d_idx, uint64_t m,
+                   void* d_out, cudaStream_t s);
+void launch_rank(ewt_tree& t, const void* d_q, uint64_t m, uint64_t* d_out,
+                 cudaStream_t s);
+void launch_select(ewt_tree& t, const void* d_q, uint64_t m, uint64_t* d_out,
+                   cudaStream_t s);
+void launch_mixed(ewt_tree& t, const uint8_t* d_types, const void* d_q,
+                  uint64_t m, uint64_t* d_out, cudaStream_t s);
+void launch_rs_rank(ewt_rs& r, int array, int value, const uint64_t* d_pos,
+                    uint64_t m, uint64_t* d_out, cudaStream_t s);
+void launch_rs_select(ewt_rs& r, int array, int value, const uint64_t* d_i,
+                      uint64_t m, uint64_t* d_out, cudaStream_t s);
+}  // namespace ewt

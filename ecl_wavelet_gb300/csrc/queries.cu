@@ -1,0 +1,264 @@
+// Batched access / rank / select kernels over a built tree, and binary
+// rank / select over a standalone RankSelect.
+//
+// One thread answers one query (the reference's ThreadsPerQuery = 1,
+// wavelet_tree.cuh:958-960).  Every CTA first stages the per-level array
+// metadata and node bases in shared memory, plus the count table and the
+// node-start ranks when they fit (the reference's ShmemOffsets / ShmemRanks
+// / ShmemCounts variants, :373-544).  The grid is sized to keep every SM
+// full and strides over the batch.  Invalid queries (select k == 0, rank
+// index > n, a symbol above the alphabet) write UINT64_MAX and raise the
+// tree's error word; access with index >= n writes 0.
+#include <algorithm>
+
+#include "internal.cuh"
+
+namespace ewt {
+
+using namespace ecl::detail;
+
+template <class T>
+struct alignas(8) QueryRec {
+  uint64_t index;
+  T symbol;
+};
+static_assert(sizeof(QueryRec<uint8_t>) == 16, "RankSelectQuery layout");
+static_assert(sizeof(QueryRec<uint64_t>) == 16, "RankSelectQuery layout");
+
+enum Kind { kAccess = 0, kRank = 1, kSelect = 2, kMixed = 3 };
+
+constexpr uint32_t kQueryThreads = 256;
+constexpr uint64_t kStageLimitBytes = 96 * 1024;
+
+struct StagePlan {
+  uint32_t stage_counts, stage_ranks;
+  size_t bytes;
+};
+
+inline StagePlan plan_stage(ewt_tree const& t) {
+  StagePlan p{0, 0, 0};
+  size_t b = t.L * sizeof(ArrayMeta) + (t.L + 1) * 8;
+  b = (b + 15) & ~size_t(15);
+  if (b + t.sigma * 8 <= kStageLimitBytes / 2) {
+    p.stage_counts = 1;
+    b += t.sigma * 8;
+  }
+  if (b + t.nodes.size() * 8 <= kStageLimitBytes) {
+    p.stage_ranks = 1;
+    b += t.nodes.size() * 8;
+  }
+  p.bytes = b;
+  return p;
+}
+
+template <class T, int K>
+__global__ void __launch_bounds__(kQueryThreads)
+query_kernel(TreeView t, uint8_t const* __restrict__ types,
+             void const* __restrict__ in, uint64_t m, void* __restrict__ out,
+             uint32_t* __restrict__ err, uint32_t stage_counts,
+             uint32_t stage_ranks) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint32_t const L = t.levels;
+  ArrayMeta* meta = reinterpret_cast<ArrayMeta*>(smem);
+  uint64_t* node_base = reinterpret_cast<uint64_t*>(meta + L);
+  size_t off = L * sizeof(ArrayMeta) + (L + 1) * 8;
+  off = (off + 15) & ~size_t(15);
+  uint64_t const* counts = t.counts;
+  uint64_t const* ranks = t.node_ranks;
+  {
+    uint64_t const* gm = reinterpret_cast<uint64_t const*>(t.rs.meta);
+    uint64_t* sm = reinterpret_cast<uint64_t*>(meta);
+    uint32_t const mw = L * (sizeof(ArrayMeta) / 8);
+    for (uint32_t i = threadIdx.x; i < mw; i += blockDim.x) sm[i] = gm[i];
+    for (uint32_t i = threadIdx.x; i <= L; i += blockDim.x)
+      node_base[i] = t.node_base[i];
+    if (stage_counts) {
+      uint64_t* sc = reinterpret_cast<uint64_t*>(smem + off);
+      for (uint64_t i = threadIdx.x; i < t.sigma; i += blockDim.x)
+        sc[i] = t.counts[i];
+      counts = sc;
+      off += t.sigma * 8;
+    }
+    if (stage_ranks) {
+      uint64_t* sr = reinterpret_cast<uint64_t*>(smem + off);
+      for (uint64_t i = threadIdx.x; i < t.num_ranks; i += blockDim.x)
+        sr[i] = t.node_ranks[i];
+      ranks = sr;
+    }
+  }
+  __syncthreads();
+  uint32_t bad = 0;
+  uint64_t const stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < m;
+       i += stride) {
+    int kind = K;
+    if (K == kMixed) kind = types[i];
+    if (kind == kAccess) {
+      uint64_t idx;
+      if (K == kMixed)
+        idx = static_cast<QueryRec<T> const*>(in)[i].index;
+      else
+        idx = static_cast<uint64_t const*>(in)[i];
+      T res = 0;
+      if (idx < t.n)
+        res = from_minimal<T>(
+            t, wt_access(t, meta, counts, ranks, node_base, idx));
+      if (K == kMixed)
+        static_cast<uint64_t*>(out)[i] = res;
+      else
+        static_cast<T*>(out)[i] = res;
+      continue;
+    }
+    QueryRec<T> const q = static_cast<QueryRec<T> const*>(in)[i];
+    uint64_t const c = to_minimal<T>(t, q.symbol);
+    uint64_t res;
+    if (kind == kRank) {
+      if (c >= t.sigma || q.index > t.n) {
+        res = UINT64_MAX;
+        bad = 1;
+      } else {
+        res = wt_rank(t, meta, counts, ranks, node_base, c, q.index);
+      }
+    } else if (kind == kSelect) {
+      if (c >= t.sigma || q.index == 0) {
+        res = UINT64_MAX;
+        bad = 1;
+      } else {
+        res = wt_select(t, meta, counts, ranks, node_base, c, q.index);
+      }
+    } else {
+      res = UINT64_MAX;
+      bad = 1;
+    }
+    static_cast<uint64_t*>(out)[i] = res;
+  }
+  if (bad) atomicOr(err, 1u);
+}
+
+template <int Value>
+__global__ void __launch_bounds__(256)
+rs_rank_kernel(RSView v, uint32_t array, uint64_t const* __restrict__ pos,
+               uint64_t m, uint64_t* __restrict__ out, uint32_t* err) {
+  ArrayMeta const meta = v.meta[array];
+  uint64_t const stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < m;
+       i += stride) {
+    uint64_t const p = pos[i];
+    if (p > meta.bits) {
+      out[i] = UINT64_MAX;
+      atomicOr(err, 1u);
+      continue;
+    }
+    uint64_t const r1 = rs_rank1<false>(v, meta, p, nullptr);
+    out[i] = Value ? r1 : p - r1;
+  }
+}
+
+template <int Value>
+__global__ void __launch_bounds__(256)
+rs_select_kernel(RSView v, uint32_t array, uint64_t const* __restrict__ idx,
+                 uint64_t m, uint64_t* __restrict__ out, uint32_t* err) {
+  ArrayMeta const meta = v.meta[array];
+  uint64_t const stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < m;
+       i += stride) {
+    uint64_t const k = idx[i];
+    if (k == 0) {
+      out[i] = UINT64_MAX;
+      atomicOr(err, 1u);
+      continue;
+    }
+    out[i] = rs_select<Value>(v, meta, k);
+  }
+}
+
+namespace {
+
+template <class T, int K>
+void launch_typed(ewt_tree& t, uint8_t const* types, void const* in,
+                  uint64_t m, void* out, cudaStream_t s) {
+  if (m == 0) return;
+  StagePlan const p = plan_stage(t);
+  auto k = query_kernel<T, K>;
+  static thread_local bool attr_set[4][4] = {};
+  int const ti = sizeof(T) == 1 ? 0 : sizeof(T) == 2 ? 1 : sizeof(T) == 4 ? 2 : 3;
+  if (!attr_set[ti][K]) {
+    EWT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(kStageLimitBytes + 4096)));
+    attr_set[ti][K] = true;
+  }
+  int per_sm = 0;
+  EWT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k,
+                                                         kQueryThreads, p.bytes));
+  per_sm = std::max(per_sm, 1);
+  uint64_t const need = ceil_div(m, kQueryThreads);
+  uint64_t const full = uint64_t(per_sm) * sm_count();
+  uint32_t const blocks = static_cast<uint32_t>(std::min(need, full));
+  PhaseTimer pt(EWT_PHASE_QUERY, s);
+  k<<<blocks, kQueryThreads, p.bytes, s>>>(t.view, types, in, m, out,
+                                           t.err_d.as<uint32_t>(),
+                                           p.stage_counts, p.stage_ranks);
+  EWT_LAUNCHED();
+}
+
+template <int K>
+void launch_any(ewt_tree& t, uint8_t const* types, void const* in, uint64_t m,
+                void* out, cudaStream_t s) {
+  switch (t.elem_size) {
+    case 1: launch_typed<uint8_t, K>(t, types, in, m, out, s); break;
+    case 2: launch_typed<uint16_t, K>(t, types, in, m, out, s); break;
+    case 4: launch_typed<uint32_t, K>(t, types, in, m, out, s); break;
+    default: launch_typed<uint64_t, K>(t, types, in, m, out, s); break;
+  }
+}
+
+uint32_t grid_for(uint64_t m) {
+  uint64_t const need = ceil_div(m, 256);
+  uint64_t const full = uint64_t(sm_count()) * 8;
+  return static_cast<uint32_t>(std::max<uint64_t>(1, std::min(need, full)));
+}
+
+}  // namespace
+
+void launch_access(ewt_tree& t, uint64_t const* d_idx, uint64_t m, void* d_out,
+                   cudaStream_t s) {
+  launch_any<kAccess>(t, nullptr, d_idx, m, d_out, s);
+}
+void launch_rank(ewt_tree& t, void const* d_q, uint64_t m, uint64_t* d_out,
+                 cudaStream_t s) {
+  launch_any<kRank>(t, nullptr, d_q, m, d_out, s);
+}
+void launch_select(ewt_tree& t, void const* d_q, uint64_t m, uint64_t* d_out,
+                   cudaStream_t s) {
+  launch_any<kSelect>(t, nullptr, d_q, m, d_out, s);
+}
+void launch_mixed(ewt_tree& t, uint8_t const* d_types, void const* d_q,
+                  uint64_t m, uint64_t* d_out, cudaStream_t s) {
+  launch_any<kMixed>(t, d_types, d_q, m, d_out, s);
+}
+
+void launch_rs_rank(ewt_rs& r, int array, int value, uint64_t const* d_pos,
+                    uint64_t m, uint64_t* d_out, cudaStream_t s) {
+  if (m == 0) return;
+  uint32_t* err = r.err_d.as<uint32_t>();
+  RSView const v = r.rs.view();
+  if (value)
+    rs_rank_kernel<1><<<grid_for(m), 256, 0, s>>>(v, array, d_pos, m, d_out, err);
+  else
+    rs_rank_kernel<0><<<grid_for(m), 256, 0, s>>>(v, array, d_pos, m, d_out, err);
+  EWT_LAUNCHED();
+}
+
+void launch_rs_select(ewt_rs& r, int array, int value, uint64_t const* d_i,
+                      uint64_t m, uint64_t* d_out, cudaStream_t s) {
+  if (m == 0) return;
+  uint32_t* err = r.err_d.as<uint32_t>();
+  RSView const v = r.rs.view();
+  if (value)
+    rs_select_kernel<1><<<grid_for(m), 256, 0, s>>>(v, array, d_i, m, d_out, err);
+  else
+    rs_select_kernel<0><<<grid_for(m), 256, 0, s>>>(v, array, d_i, m, d_out, err);
+  EWT_LAUNCHED();
+}
+
+}  // namespace ewt

@@ -1,0 +1,379 @@
+/*
+ * Device-side data views and query primitives of the GB300 wavelet tree.
+ *
+ * Shared by the library's own kernels (libewt.so) and by the drop-in C++
+ * headers, so a user kernel that receives an ecl::WaveletTree<T> by value
+ * runs exactly the code the batch kernels run.
+ *
+ * Format (kept identical to mfranzreb/ECL_wavelet so exports compare
+ * byte-for-byte):
+ *   - a bit array stores bit i in bit i%32 of uint32 word i/32
+ *     (include/ecl_wavelet/bitarray/bit_array.cuh:39-46); each array starts
+ *     on a 32-word (128-byte) boundary (src/bitarray/bit_array.cu:62-68);
+ *   - L1: uint64 count of ones before every 65,536-bit block; L2: uint16
+ *     count of ones since the enclosing L1 block, per 512-bit block; select
+ *     samples: position of every 4096-th one / zero
+ *     (include/ecl_wavelet/bitarray/rank_select.cuh:44-64).
+ */
+#pragma once
+#include <cstdint>
+
+#ifndef __CUDACC__
+#error "device_ops.cuh must be compiled by nvcc"
+#endif
+
+namespace ecl {
+namespace detail {
+
+constexpr uint64_t kL1Bits = 65536;
+constexpr uint64_t kL2Bits = 512;
+constexpr uint64_t kL2PerL1 = 128;
+constexpr uint64_t kL2Words = kL2Bits / 32;
+constexpr uint64_t kSampleRate = 4096;
+constexpr uint32_t kMaxLevels = 64;
+
+/* Per bit array bookkeeping; one entry per level of a tree. */
+struct ArrayMeta {
+  uint64_t word_off;    // first word of the array inside RSView::words
+  uint64_t bits;        // array length in bits
+  uint64_t l1_off;      // first L1 entry
+  uint64_t l2_off;      // first L2 entry
+  uint64_t s0_off;      // first zero-sample
+  uint64_t s1_off;      // first one-sample
+  uint64_t ones;        // total number of ones
+  uint64_t num_l1;      // number of L1 blocks
+  uint64_t num_last_l2; // L2 blocks inside the last L1 block
+};
+
+/* A set of bit arrays with rank/select support, all in device memory. */
+struct RSView {
+  const uint32_t* words;
+  const uint64_t* l1;
+  const uint16_t* l2;
+  const uint64_t* s0;
+  const uint64_t* s1;
+  const ArrayMeta* meta;  // device array of num_arrays entries
+  uint32_t num_arrays;
+  uint32_t reserved;
+};
+
+/* Everything a query walk needs; trivially copyable into a kernel. */
+struct TreeView {
+  RSView rs;
+  const uint64_t* counts;          // C[c]: symbols smaller than c, sigma entries
+  const uint64_t* node_ranks;      // rank0 at every node start, num_ranks
+  const uint64_t* node_base;       // node starts on levels < l, levels + 1
+  const uint64_t* nodes_at_level;  // node starts on level l, levels
+  const uint64_t* code_len;        // short codes of symbols >= codes_start
+  const uint64_t* code_bits;
+  const void* alphabet;            // sorted original symbols, elem_size each
+  uint64_t n;
+  uint64_t sigma;
+  uint64_t codes_start;
+  uint64_t num_ranks;
+  uint64_t num_nodes_until_last_level;
+  uint32_t levels;
+  uint32_t elem_size;
+  uint32_t is_pow2;
+  uint32_t is_min;
+};
+
+/* ---------------------------------------------------------------------- */
+__device__ __forceinline__ uint32_t popc32(uint32_t x) { return __popc(x); }
+
+__device__ __forceinline__ bool is_pow2_u64(uint64_t n) {
+  return (n & (n - 1)) == 0;
+}
+
+/* n/2 for powers of two, else the largest power of two below n
+ * (semantics of utils.cuh:123-146 getPrevPowTwo). */
+__device__ __forceinline__ uint64_t prev_pow2_u64(uint64_t n) {
+  if (n == 0) return 0;
+  if (is_pow2_u64(n)) return n >> 1;
+  return uint64_t(1) << (63 - __clzll(static_cast<long long>(n)));
+}
+
+/* Position (0-based) of the r-th (1-based) set bit of x; r <= popc(x). */
+__device__ __forceinline__ uint32_t select_in_word(uint32_t x, uint32_t r) {
+  uint32_t pos = 0;
+  uint32_t c = __popc(x & 0xFFFFu);
+  if (r > c) { r -= c; x >>= 16; pos += 16; }
+  c = __popc(x & 0xFFu);
+  if (r > c) { r -= c; x >>= 8; pos += 8; }
+  c = __popc(x & 0xFu);
+  if (r > c) { r -= c; x >>= 4; pos += 4; }
+  c = __popc(x & 0x3u);
+  if (r > c) { r -= c; x >>= 2; pos += 2; }
+  c = x & 1u;
+  if (r > c) pos += 1;
+  return pos;
+}
+
+__device__ __forceinline__ bool rs_bit(const RSView& v, const ArrayMeta& m,
+                                       uint64_t pos) {
+  return (__ldg(v.words + m.word_off + (pos >> 5)) >> (pos & 31)) & 1u;
+}
+
+/* Ones in [0, pos) of one array, pos <= bits; with GetBit also the bit at
+ * pos (false for pos == bits).  Loads the L1 entry, the L2 entry and the
+ * 128-bit chunks of the 512-bit block up to pos, all independent. */
+template <bool GetBit>
+__device__ __forceinline__ uint64_t rs_rank1(const RSView& v,
+                                             const ArrayMeta& m, uint64_t pos,
+                                             bool* bit) {
+  if (pos >= m.bits) {
+    if (GetBit) *bit = false;
+    return m.ones;
+  }
+  uint64_t const b2 = pos >> 9;
+  uint64_t r = __ldg(v.l1 + m.l1_off + (pos >> 16));
+  r += __ldg(v.l2 + m.l2_off + b2);
+  uint4 const* blk =
+      reinterpret_cast<uint4 const*>(v.words + m.word_off + b2 * kL2Words);
+  uint32_t const off = static_cast<uint32_t>(pos & 511);
+  uint32_t const last = off >> 7;
+  uint32_t acc = 0;
+#pragma unroll
+  for (uint32_t j = 0; j < 4; ++j) {
+    if (j < last) {
+      uint4 const q = __ldg(blk + j);
+      acc += __popc(q.x) + __popc(q.y) + __popc(q.z) + __popc(q.w);
+    } else if (j == last && (GetBit || (off & 127) != 0)) {
+      uint4 const q = __ldg(blk + j);
+      uint32_t const o = off & 127;
+      uint32_t const wi = o >> 5;
+      uint32_t const w = wi == 0 ? q.x : wi == 1 ? q.y : wi == 2 ? q.z : q.w;
+      acc += (wi > 0 ? __popc(q.x) : 0) + (wi > 1 ? __popc(q.y) : 0) +
+             (wi > 2 ? __popc(q.z) : 0);
+      acc += __popc(w & ((1u << (o & 31)) - 1u));
+      if (GetBit) *bit = (w >> (o & 31)) & 1u;
+    }
+  }
+  return r + acc;
+}
+
+/* Position of the i-th (1-based) `Value` bit, or bits when there are fewer
+ * (or i == 0).  Sample bracket -> L1 binary search -> L2 binary search in
+ * the bracketed range -> scan of the 512-bit block -> in-word select. */
+template <int Value>
+__device__ __forceinline__ uint64_t rs_select(const RSView& v,
+                                              const ArrayMeta& m, uint64_t i) {
+  uint64_t const total = Value ? m.ones : m.bits - m.ones;
+  if (i == 0 || i > total) return m.bits;
+  uint64_t const* S = Value ? v.s1 + m.s1_off : v.s0 + m.s0_off;
+  uint64_t const q = i / kSampleRate;
+  uint64_t const lo = q ? __ldg(S + q - 1) : 0;
+  uint64_t const hi = (q + 1) * kSampleRate <= total ? __ldg(S + q) : m.bits - 1;
+  uint64_t const* L1 = v.l1 + m.l1_off;
+  uint64_t b_lo = lo >> 16, b_hi = hi >> 16;
+  // Invariant: values before block b_lo < i.
+  while (b_lo < b_hi) {
+    uint64_t const mid = (b_lo + b_hi + 1) >> 1;
+    uint64_t const x = __ldg(L1 + mid);
+    uint64_t const before = Value ? x : (mid << 16) - x;
+    if (before < i) b_lo = mid; else b_hi = mid - 1;
+  }
+  uint64_t const b = b_lo;
+  uint64_t const xb = __ldg(L1 + b);
+  uint64_t rem = i - (Value ? xb : (b << 16) - xb);
+  uint64_t const first = b * kL2PerL1;
+  uint64_t const num_l2 = (m.num_l1 - 1) * kL2PerL1 + m.num_last_l2;
+  uint64_t k_lo = ((lo >> 16) == b) ? (lo >> 9) : first;
+  uint64_t k_hi = first + kL2PerL1 - 1;
+  if (k_hi > num_l2 - 1) k_hi = num_l2 - 1;
+  if ((hi >> 16) == b && (hi >> 9) < k_hi) k_hi = hi >> 9;
+  uint16_t const* L2 = v.l2 + m.l2_off;
+  while (k_lo < k_hi) {
+    uint64_t const mid = (k_lo + k_hi + 1) >> 1;
+    uint32_t const x = __ldg(L2 + mid);
+    uint64_t const before = Value ? x : ((mid - first) << 9) - x;
+    if (before < rem) k_lo = mid; else k_hi = mid - 1;
+  }
+  uint32_t const xk = __ldg(L2 + k_lo);
+  rem -= Value ? xk : ((k_lo - first) << 9) - xk;
+  uint4 const* blk =
+      reinterpret_cast<uint4 const*>(v.words + m.word_off + k_lo * kL2Words);
+  uint4 qs[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) qs[j] = __ldg(blk + j);
+  uint32_t r = static_cast<uint32_t>(rem);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    uint32_t ws[4] = {qs[j].x, qs[j].y, qs[j].z, qs[j].w};
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      uint32_t const w = Value ? ws[t] : ~ws[t];
+      uint32_t const c = __popc(w);
+      if (r <= c) {
+        return (k_lo * kL2Words + j * 4 + t) * 32 + select_in_word(w, r);
+      }
+      r -= c;
+    }
+  }
+  return m.bits;  // not reached for valid structures
+}
+
+/* ---- tree walks ------------------------------------------------------- */
+
+/* Index into node_ranks of the node starting at symbol cs on level l >= 1
+ * (getNodePosAtLevel, wavelet_tree.cuh:2241-2268, plus the per-level base
+ * the reference accumulates in ranks_start). */
+__device__ __forceinline__ uint64_t node_index(const TreeView& t,
+                                               uint64_t const* node_base,
+                                               uint64_t cs, uint32_t l) {
+  uint64_t pos;
+  if (l == 1) {
+    pos = 0;
+  } else if (t.is_pow2) {
+    pos = (cs >> (t.levels - l)) - 1;
+  } else {
+    uint64_t num_prev = 0, node_lens = 1, remaining = t.sigma, sym = cs;
+    for (int i = int(l) - 1; i >= 0; --i) {
+      uint64_t const sub = prev_pow2_u64(remaining);
+      node_lens = sub >> i;
+      if (sym <= sub) break;
+      remaining -= sub;
+      num_prev += sub / node_lens;
+      sym -= sub;
+    }
+    pos = sym / node_lens + num_prev - 1;
+  }
+  return node_base[l] + pos;
+}
+
+__device__ __forceinline__ uint64_t occurrences(const TreeView& t,
+                                                uint64_t const* counts,
+                                                uint64_t c) {
+  return (c + 1 == t.sigma ? t.n : counts[c + 1]) - counts[c];
+}
+
+/* Minimal symbol at text position idx < n (deviceAccess,
+ * wavelet_tree.cuh:1815-1877). */
+__device__ __forceinline__ uint64_t wt_access(const TreeView& t,
+                                              ArrayMeta const* meta,
+                                              uint64_t const* counts,
+                                              uint64_t const* ranks,
+                                              uint64_t const* node_base,
+                                              uint64_t idx) {
+  uint64_t cs = 0, ce = t.sigma - 1;
+  for (uint32_t l = 0; l < t.levels; ++l) {
+    ArrayMeta const& m = meta[l];
+    uint64_t const cc = counts[cs];
+    if (ce - cs < 2) {
+      if (ce - cs > 0 && rs_bit(t.rs, m, cc + idx)) cs++;
+      break;
+    }
+    uint64_t const start = cs ? ranks[node_index(t, node_base, cs, l)] : 0;
+    uint64_t const p = cc + idx;
+    bool b;
+    uint64_t const r0 = p - rs_rank1<true>(t.rs, m, p, &b);
+    uint64_t const diff = prev_pow2_u64(ce - cs + 1);
+    if (!b) {
+      idx = r0 - start;
+      ce = cs + diff - 1;
+    } else {
+      idx -= r0 - start;
+      cs += diff;
+    }
+  }
+  return cs;
+}
+
+/* Occurrences of minimal symbol c in [0, i), i <= n (deviceRank,
+ * wavelet_tree.cuh:1896-1956; zero-count shortcut :481-486). */
+__device__ __forceinline__ uint64_t wt_rank(const TreeView& t,
+                                            ArrayMeta const* meta,
+                                            uint64_t const* counts,
+                                            uint64_t const* ranks,
+                                            uint64_t const* node_base,
+                                            uint64_t c, uint64_t i) {
+  if (occurrences(t, counts, c) == 0) return 0;
+  uint64_t cs = 0, ce = t.sigma - 1, res = i;
+  for (uint32_t l = 0; l < t.levels; ++l) {
+    if (ce == cs) break;
+    ArrayMeta const& m = meta[l];
+    uint64_t const cc = counts[cs];
+    uint64_t const start = cs ? ranks[node_index(t, node_base, cs, l)] : 0;
+    uint64_t const p = cc + res;
+    uint64_t const r0 = p - rs_rank1<false>(t.rs, m, p, nullptr);
+    uint64_t const split = cs + prev_pow2_u64(ce - cs + 1);
+    if (c < split) {
+      res = r0 - start;
+      ce = split - 1;
+    } else {
+      res -= r0 - start;
+      cs = split;
+    }
+  }
+  return res;
+}
+
+/* Position of the k-th (1-based) occurrence of minimal symbol c, or n when
+ * there are fewer (deviceSelect :2007-2079, getPrevCharStart :1970-1992,
+ * k > count check :532-536). */
+__device__ __forceinline__ uint64_t wt_select(const TreeView& t,
+                                              ArrayMeta const* meta,
+                                              uint64_t const* counts,
+                                              uint64_t const* ranks,
+                                              uint64_t const* node_base,
+                                              uint64_t c, uint64_t k) {
+  if (k == 0 || k > occurrences(t, counts, c)) return t.n;
+  uint32_t const L = t.levels;
+  uint64_t len = L, code = c;
+  if (!t.is_pow2 && c >= t.codes_start) {
+    len = t.code_len[c - t.codes_start];
+    code = t.code_bits[c - t.codes_start];
+  }
+  uint64_t res = k, cs = c;
+  for (int l = int(len) - 1; l >= 0; --l) {
+    ArrayMeta const& m = meta[l];
+    uint64_t start;
+    if ((code >> (L - 1 - l)) & 1u) {
+      if (t.is_pow2) {
+        uint64_t const node_lens = uint64_t(1) << (L - l);
+        cs &= ~(node_lens - 1);
+      } else {
+        uint64_t const top = (L - l >= 64) ? 0 : (code >> (L - l));
+        if (__popcll(top) == l) {
+          uint64_t ns = 0;
+          for (int j = 0; j < l; ++j) ns += prev_pow2_u64(t.sigma - ns);
+          cs = ns;
+        } else {
+          cs -= uint64_t(1) << (len - 1 - l);
+        }
+      }
+      start = cs ? counts[cs] - ranks[node_index(t, node_base, cs, l)] : 0;
+      res = rs_select<1>(t.rs, m, start + res) + 1;
+    } else {
+      start = cs ? ranks[node_index(t, node_base, cs, l)] : 0;
+      res = rs_select<0>(t.rs, m, start + res) + 1;
+    }
+    if (uint64_t(l) == len - 1 && res > m.bits) return t.n;
+    res -= counts[cs];
+  }
+  return res - 1;
+}
+
+/* lower_bound of s in the sorted device alphabet (the reference's host-side
+ * query remap, wavelet_tree.cuh:1425-1436).  Returns sigma if s is above
+ * the last symbol. */
+template <class T>
+__device__ __forceinline__ uint64_t to_minimal(const TreeView& t, T s) {
+  if (t.is_min) return static_cast<uint64_t>(s) < t.sigma ? s : t.sigma;
+  T const* a = static_cast<T const*>(t.alphabet);
+  uint64_t lo = 0, hi = t.sigma;
+  while (lo < hi) {
+    uint64_t const mid = (lo + hi) >> 1;
+    if (__ldg(a + mid) < s) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+template <class T>
+__device__ __forceinline__ T from_minimal(const TreeView& t, uint64_t c) {
+  if (t.is_min) return static_cast<T>(c);
+  return __ldg(static_cast<T const*>(t.alphabet) + c);
+}
+
+}  // namespace detail
+}  // namespace ecl

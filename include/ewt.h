@@ -109,11 +109,6 @@ int ewt_build_u32(const uint32_t* data, uint64_t n, const uint32_t* alphabet,
                   uint64_t sigma, uint32_t gpu_index, ewt_tree** out);
 int ewt_build_u64(const uint64_t* data, uint64_t n, const uint64_t* alphabet,
                   uint64_t sigma, uint32_t gpu_index, ewt_tree** out);
-/* Same as ewt_build but asynchronous on `stream` for a device-resident text;
- * the returned tree is usable on that stream once this returns.           */
-int ewt_build_device_async(const void* d_data, uint64_t n, int elem_size,
-                           const void* alphabet, uint64_t sigma,
-                           int gpu_index, void* stream, ewt_tree** out);
 int ewt_free(ewt_tree* tree);
 int ewt_get_info(const ewt_tree* tree, ewt_info* info);
 int ewt_export(const ewt_tree* tree, int component, int level, void* host_buf,
@@ -175,6 +170,26 @@ int ewt_rs_get_device_view(const ewt_rs* rs, void* view_out,
                            uint64_t view_size);
 
 /* ---- diagnostics ------------------------------------------------------- */
+/* Per-phase device time, measured with CUDA events recorded on the stream
+ * each kernel is launched on.  Off by default; enabling adds a stream
+ * synchronisation after every timed phase. */
+#define EWT_PHASE_HIST 0       /* histogram + remap                       */
+#define EWT_PHASE_FILL 1       /* level bit packing                        */
+#define EWT_PHASE_RS_COUNTS 2  /* L2/L1 counts + L1 scan                   */
+#define EWT_PHASE_SPLIT 3      /* per-level stable partition               */
+#define EWT_PHASE_NODE_RANKS 4 /* rank0 at node starts                     */
+#define EWT_PHASE_SAMPLES 5    /* select samples                           */
+#define EWT_PHASE_QUERY 6      /* query kernels                            */
+#define EWT_PHASE_H2D 7        /* host-to-device text copy                 */
+#define EWT_NUM_PHASES 8
+typedef struct ewt_phase_times {
+  double ms[EWT_NUM_PHASES];        /* accumulated device milliseconds    */
+  uint64_t launches[EWT_NUM_PHASES]; /* timed launches per phase          */
+} ewt_phase_times;
+void ewt_set_timing(int enable);
+/* Copies the accumulated times; resets them when reset != 0. */
+void ewt_get_timing(ewt_phase_times* out, int reset);
+
 const char* ewt_last_error(void); /* message of the calling thread's last
                                      failed call, "" if none              */
 int ewt_abi_version(void);

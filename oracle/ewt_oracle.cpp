@@ -419,7 +419,8 @@ int build_tree(Tree& t, const void* data, uint64_t n, int es,
   t.nodes = node_infos(t.sigma, t.codes);
   // :703-724 nodes per level (counted the reference's way) and the number
   // of node starts above the last level.
-  t.nodes_at_level.assign(t.L > 0 ? t.L - 1 : 0, 0);
+  // Entry L-1 (never read by the reference) holds the last level's count.
+  t.nodes_at_level.assign(t.L, 0);
   if (!t.pow2) {
     uint64_t counter = 0;
     for (uint64_t i = 0; i < t.nodes.size(); ++i) {
@@ -429,8 +430,11 @@ int build_tree(Tree& t, const void* data, uint64_t n, int es,
       }
       counter++;
     }
+    if (!t.nodes.empty() && t.nodes.back().level == t.L - 1)
+      t.nodes_at_level[t.L - 1] = counter;
     t.nodes_until_last = 0;
-    for (auto v : t.nodes_at_level) t.nodes_until_last += v;
+    for (uint32_t l = 0; l + 1 < t.L; ++l)
+      t.nodes_until_last += t.nodes_at_level[l];
   } else {
     t.nodes_until_last =
         t.nodes.size() - ((uint64_t(1) << (t.L - 1)) - 1);

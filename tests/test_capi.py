@@ -1,0 +1,55 @@
+"""The C-ABI library builds for sm_103a, loads without a GPU, and exports
+every entry point include/ewt.h declares (no compute calls here)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    src = open(os.path.join(REPO, "include", "ewt.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(ewt_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for must in ("ewt_build", "ewt_access", "ewt_rank", "ewt_select",
+                 "ewt_mixed", "ewt_export", "ewt_free", "ewt_rs_build"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(ewt):
+    lib = ctypes.CDLL(ewt.LIB_PATH)
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    assert lib.ewt_abi_version() == 1
+
+
+def test_python_binding_covers_header(ewt):
+    assert set(declared_functions()) <= set(ewt.SIGNATURES)
+
+
+def test_library_is_sm103a_only(ewt):
+    out = subprocess.run(["cuobjdump", "--list-elf", ewt.LIB_PATH],
+                         capture_output=True, text=True)
+    if out.returncode != 0:
+        pytest.skip("cuobjdump unavailable")
+    assert "sm_103a" in out.stdout
+
+
+def test_errors_without_gpu_are_statuses(ewt):
+    import numpy as np
+    lib = ewt.lib()
+    h = ctypes.c_void_p()
+    st = lib.ewt_build(None, 0, 1, None, 0, 0, ctypes.byref(h))
+    assert st == -1  # invalid argument, checked before touching a device
+    assert b"non-empty" in lib.ewt_last_error()
+    assert lib.ewt_free(None) == 0
+    st = lib.ewt_build(np.zeros(4, np.uint8).ctypes.data, 4, 3, None, 0, 0,
+                       ctypes.byref(h))
+    assert st == -1
