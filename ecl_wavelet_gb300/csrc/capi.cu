@@ -457,6 +457,7 @@ int ewt_rs_build(const uint32_t* words, const uint64_t* bits,
     r->err_d.alloc(16);
     EWT_CUDA(cudaMemset(r->err_d.get(), 0, 16));
     r->rs.layout(b);
+    if (is_device_pointer(words)) EWT_CUDA(cudaDeviceSynchronize());
     uint64_t off = 0;
     for (uint32_t a = 0; a < num_arrays; ++a) {
       uint64_t const w = ceil_div(b[a], 32);

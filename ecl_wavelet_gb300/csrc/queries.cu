@@ -28,7 +28,9 @@ static_assert(sizeof(QueryRec<uint64_t>) == 16, "RankSelectQuery layout");
 enum Kind { kAccess = 0, kRank = 1, kSelect = 2, kMixed = 3 };
 
 constexpr uint32_t kQueryThreads = 256;
-constexpr uint64_t kStageLimitBytes = 96 * 1024;
+// Staging budget per CTA: small enough that 8 CTAs (2048 threads) fit on an
+// SM's 228 KB of shared memory.
+constexpr uint64_t kStageLimitBytes = 24 * 1024;
 
 struct StagePlan {
   uint32_t stage_counts, stage_ranks;
@@ -178,6 +180,13 @@ template <class T, int K>
 void launch_typed(ewt_tree& t, uint8_t const* types, void const* in,
                   uint64_t m, void* out, cudaStream_t s) {
   if (m == 0) return;
+  EWT_REQUIRE(in != nullptr && out != nullptr && (K != kMixed || types),
+              EWT_ERR_INVALID_ARGUMENT, "null query, type or result buffer");
+  EWT_REQUIRE(reinterpret_cast<uintptr_t>(in) % 8 == 0 &&
+                  (K == kAccess ||
+                   reinterpret_cast<uintptr_t>(out) % 8 == 0),
+              EWT_ERR_INVALID_ARGUMENT,
+              "query and result buffers must be 8-byte aligned");
   StagePlan const p = plan_stage(t);
   auto k = query_kernel<T, K>;
   static thread_local bool attr_set[4][4] = {};

@@ -260,7 +260,8 @@ constexpr uint32_t kSplitTile = kSplitThreads * kSplitItems;
 template <class T, bool Pow2>
 __global__ void __launch_bounds__(kSplitThreads)
 split_level_kernel(T const* __restrict__ src, T* __restrict__ dst, uint64_t n,
-                   uint64_t size_l, uint32_t l, TreeView t) {
+                   uint64_t size_l, uint32_t l, TreeView t,
+                   uint32_t* __restrict__ err) {
   extern __shared__ __align__(16) unsigned char smem[];
   uint64_t* dests = reinterpret_cast<uint64_t*>(smem);
   T* vals = reinterpret_cast<T*>(smem + kSplitTile * sizeof(uint64_t));
@@ -343,10 +344,15 @@ split_level_kernel(T const* __restrict__ src, T* __restrict__ dst, uint64_t n,
       uint64_t const ca = counts[nr.cs];
       uint64_t const cm = counts[nr.split];
       uint64_t const cend = (nr.ce + 1 >= t.sigma) ? t.n : counts[nr.ce + 1];
-      uint64_t const zn =
-          nr.cs == 0 ? 0
-                     : t.node_ranks[ecl::detail::node_index(t, t.node_base,
-                                                            nr.cs, l)];
+      uint64_t zn = 0;
+      if (nr.cs != 0) {
+        uint64_t const ni = ecl::detail::node_index(t, t.node_base, nr.cs, l);
+        if (ni < t.num_ranks) zn = t.node_ranks[ni];
+        else {
+          atomicOr(err, 2u);
+          atomicMin(err + 1, blockIdx.x);
+        }
+      }
       uint64_t const f = max(ca, tile_start);
       uint64_t const zf = ca > tile_start ? zn : z_tile;
       uint64_t const ze =
@@ -359,12 +365,22 @@ split_level_kernel(T const* __restrict__ src, T* __restrict__ dst, uint64_t n,
       slot = p - tile_start;
       dest = p;
     }
+    // Consistency guard: a slot or destination outside the tile / text
+    // means corrupt bookkeeping; record it instead of writing out of range.
+    if (slot >= kSplitTile || dest >= n) {
+      atomicOr(err, slot >= kSplitTile ? 4u : 8u);
+      atomicMin(err + 1, blockIdx.x);
+      continue;
+    }
     dests[slot] = dest;
     vals[slot] = item[j];
   }
   __syncthreads();
   uint32_t const cnt = static_cast<uint32_t>(tile_end - tile_start);
-  for (uint32_t s = tid; s < cnt; s += kSplitThreads) dst[dests[s]] = vals[s];
+  for (uint32_t s = tid; s < cnt; s += kSplitThreads) {
+    uint64_t const d = dests[s];
+    if (d < n) dst[d] = vals[s];
+  }
 }
 
 template <class T>
@@ -376,8 +392,17 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   DevBuf text_owned;
   T const* d_text;
   bool const on_device = is_device_pointer(data);
-  if (on_device) {
+  // The text may still be in flight on the caller's streams; the build runs
+  // on its own stream, so order it after all prior device work.
+  if (on_device) EWT_CUDA(cudaDeviceSynchronize());
+  if (on_device && reinterpret_cast<uintptr_t>(data) % 16 == 0) {
     d_text = static_cast<T const*>(data);
+  } else if (on_device) {
+    // The kernels read the text with 16-byte vector loads.
+    text_owned.alloc(n * sizeof(T));
+    EWT_CUDA(cudaMemcpyAsync(text_owned.get(), data, n * sizeof(T),
+                             cudaMemcpyDeviceToDevice, st));
+    d_text = text_owned.as<T>();
   } else {
     text_owned.alloc(n * sizeof(T));
     PhaseTimer pt(EWT_PHASE_H2D, st);
@@ -466,6 +491,7 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   // ---- device tables
   t.err_d.alloc(16);
   EWT_CUDA(cudaMemsetAsync(t.err_d.get(), 0, 16, st));
+  EWT_CUDA(cudaMemsetAsync(t.err_d.as<uint32_t>() + 2, 0xFF, 4, st));
   DevBuf cur_buf;  // remapped text when the alphabet is not 0..sigma-1
   if (!t.is_min) {
     std::vector<T> a(t.alphabet.begin(), t.alphabet.end());
@@ -596,9 +622,19 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
       T* dst = bufs[l & 1];
       PhaseTimer pt(EWT_PHASE_SPLIT, st);
       split_k<<<static_cast<uint32_t>(ceil_div(n, kSplitTile)), kSplitThreads,
-                split_smem, st>>>(src, dst, n, size_l, l, v);
+                split_smem, st>>>(src, dst, n, size_l, l, v,
+                                  t.err_d.as<uint32_t>() + 1);
       EWT_LAUNCHED();
       src = dst;
+      uint32_t build_err[2] = {0, 0};
+      EWT_CUDA(cudaMemcpyAsync(build_err, t.err_d.as<uint32_t>() + 1, 8,
+                               cudaMemcpyDeviceToHost, st));
+      EWT_CUDA(cudaStreamSynchronize(st));
+      EWT_REQUIRE(build_err[0] == 0, EWT_ERR_CUDA,
+                  "internal consistency check failed while partitioning "
+                  "level " + std::to_string(l) + " (kind " +
+                      std::to_string(build_err[0]) + ", first tile " +
+                      std::to_string(build_err[1]) + ")");
     }
   }
   build_rs_samples(t.rs, st);

@@ -96,6 +96,9 @@ typedef struct ewt_rs ewt_rs;     /* opaque standalone RankSelect */
 
 /* ---- construction ------------------------------------------------------
  * data: n symbols of elem_size bytes (1, 2, 4 or 8), host OR device memory.
+ * A device-resident text is read after a device-wide synchronisation, so
+ * work still writing it on any stream completes first.  The call returns
+ * once the tree is built.
  * alphabet: sorted distinct symbols in host memory (elem_size bytes each), or
  * NULL with sigma == 0 to detect the alphabet from the text.               */
 int ewt_build(const void* data, uint64_t n, int elem_size,
