@@ -19,7 +19,7 @@ using ecl::detail::TreeView;
 // do: arrays padded to 32-word multiples, total word count even.
 struct RSStore {
   std::vector<ArrayMeta> meta;  // host copy
-  DevBuf words, l1, l2, s0, s1, meta_d;
+  DevBuf words, l1, l2, s0, s1, meta_d, jobs_d;
   uint64_t total_words = 0, total_l1 = 0, total_l2 = 0;
   uint64_t total_s0 = 0, total_s1 = 0;
 
@@ -34,7 +34,8 @@ struct RSStore {
 };
 
 // Builds L2/L1/total counts for arrays [first, last) of `rs` on `stream`
-// (the words must be final), copies totals to the host meta.
+// (the words must be final); totals land in the device meta table only.
+// Asynchronous: no host synchronisation.
 void build_rs_counts(RSStore& rs, uint32_t first, uint32_t last,
                      cudaStream_t stream);
 // Allocates and fills the select samples of every array (needs counts of

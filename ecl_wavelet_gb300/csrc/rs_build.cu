@@ -21,6 +21,10 @@ using ecl::detail::kL2PerL1;
 using ecl::detail::kL2Words;
 using ecl::detail::kSampleRate;
 
+struct BlockJob {
+  uint64_t word_off, bits, l2_off, l1_off, num_l1, num_last_l2;
+};
+
 void RSStore::layout(std::vector<uint64_t> const& bits) {
   meta.assign(bits.size(), ArrayMeta{});
   total_words = total_l1 = total_l2 = 0;
@@ -43,6 +47,15 @@ void RSStore::layout(std::vector<uint64_t> const& bits) {
   l1.alloc(total_l1 * 8);
   l2.alloc(total_l2 * 2);
   meta_d.alloc(meta.size() * sizeof(ArrayMeta));
+  EWT_CUDA(cudaMemcpy(meta_d.get(), meta.data(), meta.size() * sizeof(ArrayMeta),
+                      cudaMemcpyHostToDevice));
+  std::vector<BlockJob> jobs(meta.size());
+  for (size_t a = 0; a < meta.size(); ++a)
+    jobs[a] = {meta[a].word_off, meta[a].bits, meta[a].l2_off, meta[a].l1_off,
+               meta[a].num_l1, meta[a].num_last_l2};
+  jobs_d.alloc(jobs.size() * sizeof(BlockJob));
+  EWT_CUDA(cudaMemcpy(jobs_d.get(), jobs.data(), jobs.size() * sizeof(BlockJob),
+                      cudaMemcpyHostToDevice));
   // Zero the padding words behind every array (the arrays themselves are
   // written completely by their producer).
   for (auto const& m : meta) {
@@ -69,10 +82,6 @@ RSView RSStore::view() const {
 }
 
 namespace {
-
-struct BlockJob {
-  uint64_t word_off, bits, l2_off, l1_off, num_l1, num_last_l2;
-};
 
 // Finds the array owning global L1 block g among jobs[0..count).
 __device__ __forceinline__ uint32_t find_job(BlockJob const* jobs,
@@ -135,10 +144,11 @@ rs_block_kernel(uint32_t const* __restrict__ words, BlockJob const* jobs,
   if (k == 127) l1[job.l1_off + b] = base + inc;  // block total for now
 }
 
-// One CTA per array: in-place exclusive scan of the L1 block totals.
+// One CTA per array: in-place exclusive scan of the L1 block totals; the
+// grand total goes straight into the array's device meta entry.
 __global__ void __launch_bounds__(1024)
-rs_l1_scan_kernel(BlockJob const* jobs, uint64_t* __restrict__ l1,
-                  uint64_t* __restrict__ ones_out) {
+rs_l1_scan_kernel(BlockJob const* jobs, uint32_t first_array,
+                  uint64_t* __restrict__ l1, ArrayMeta* __restrict__ meta) {
   BlockJob const job = jobs[blockIdx.x];
   uint64_t* p = l1 + job.l1_off;
   __shared__ uint64_t warp_tot[32];
@@ -165,7 +175,7 @@ rs_l1_scan_kernel(BlockJob const* jobs, uint64_t* __restrict__ l1,
     if (t == blockDim.x - 1) carry_s = carry + wb + inc;
     __syncthreads();
   }
-  if (t == 0) ones_out[blockIdx.x] = carry_s;
+  if (t == 0) meta[first_array + blockIdx.x].ones = carry_s;
 }
 
 struct SampleJob {
@@ -237,43 +247,30 @@ void build_rs_counts(RSStore& rs, uint32_t first, uint32_t last,
                      cudaStream_t stream) {
   if (first >= last) return;
   uint32_t const count = last - first;
-  std::vector<BlockJob> jobs(count);
-  for (uint32_t a = first; a < last; ++a) {
-    ArrayMeta const& m = rs.meta[a];
-    jobs[a - first] = {m.word_off, m.bits, m.l2_off, m.l1_off, m.num_l1,
-                       m.num_last_l2};
-  }
-  DevBuf jobs_d(count * sizeof(BlockJob));
-  DevBuf ones_d(count * sizeof(uint64_t));
-  EWT_CUDA(cudaMemcpyAsync(jobs_d.get(), jobs.data(), count * sizeof(BlockJob),
-                           cudaMemcpyHostToDevice, stream));
+  BlockJob const* jobs = rs.jobs_d.as<BlockJob>() + first;
   PhaseTimer pt(EWT_PHASE_RS_COUNTS, stream);
   uint64_t const l1_first = rs.meta[first].l1_off;
   uint64_t const l1_end = rs.meta[last - 1].l1_off + rs.meta[last - 1].num_l1;
   for (uint64_t base = l1_first; base < l1_end; base += (1u << 30)) {
     uint64_t const nb = std::min<uint64_t>(l1_end - base, 1u << 30);
     rs_block_kernel<<<static_cast<uint32_t>(nb), 128, 0, stream>>>(
-        rs.words.as<uint32_t>(), jobs_d.as<BlockJob>(), count, base,
-        rs.l2.as<uint16_t>(), rs.l1.as<uint64_t>());
+        rs.words.as<uint32_t>(), jobs, count, base, rs.l2.as<uint16_t>(),
+        rs.l1.as<uint64_t>());
     EWT_LAUNCHED();
   }
   rs_l1_scan_kernel<<<count, 1024, 0, stream>>>(
-      jobs_d.as<BlockJob>(), rs.l1.as<uint64_t>(), ones_d.as<uint64_t>());
+      jobs, first, rs.l1.as<uint64_t>(), rs.meta_d.as<ArrayMeta>());
   EWT_LAUNCHED();
-  std::vector<uint64_t> ones(count);
-  EWT_CUDA(cudaMemcpyAsync(ones.data(), ones_d.get(), count * 8,
-                           cudaMemcpyDeviceToHost, stream));
-  EWT_CUDA(cudaStreamSynchronize(stream));
-  for (uint32_t a = first; a < last; ++a) rs.meta[a].ones = ones[a - first];
-  // Keep the device meta current so rank works between levels.
-  EWT_CUDA(cudaMemcpyAsync(rs.meta_d.as<ArrayMeta>() + first, &rs.meta[first],
-                           count * sizeof(ArrayMeta), cudaMemcpyHostToDevice,
-                           stream));
-  EWT_CUDA(cudaStreamSynchronize(stream));
 }
 
 void build_rs_samples(RSStore& rs, cudaStream_t stream) {
   uint32_t const count = static_cast<uint32_t>(rs.meta.size());
+  // Totals of ones were written on the device by the L1 scans.
+  std::vector<ArrayMeta> dm(count);
+  EWT_CUDA(cudaMemcpyAsync(dm.data(), rs.meta_d.get(), count * sizeof(ArrayMeta),
+                           cudaMemcpyDeviceToHost, stream));
+  EWT_CUDA(cudaStreamSynchronize(stream));
+  for (uint32_t a = 0; a < count; ++a) rs.meta[a].ones = dm[a].ones;
   rs.total_s0 = rs.total_s1 = 0;
   for (auto& m : rs.meta) {
     m.s1_off = rs.total_s1;

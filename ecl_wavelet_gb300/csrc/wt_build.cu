@@ -1,24 +1,34 @@
 // Wavelet-tree construction on the GPU.
 //
-// Pipeline (one GPU, one stream; host code orchestrates):
+// Pipeline (one GPU, one stream, no host round trip between levels):
 //   1. alphabet: given, or detected (presence bitmap kernel for 1/2-byte
 //      symbols, host sort for wider ones) — wavelet_tree.cuh:590-614;
 //   2. shape on the host: minimal codes for non-power-of-two alphabets
-//      (:2100-2159), node starts (:2501-2532), nodes per level (:703-724);
-//   3. histogram kernel: occurrences per minimal symbol, and for a
-//      non-minimal alphabet the remapped text (:170-227, :2295-2413);
-//   4. for every level l: fill kernel packs the level's bits (bit L-1-l of
-//      each symbol, in level order) into words; RankSelect counts of the
-//      level; rank0 at the level's node starts (:332-352); then the split
-//      kernel stably partitions every node of level l by its bit, which
-//      yields the level l+1 order (the reference re-sorts the whole text on
-//      the top l+1 code bits with cub::DeviceRadixSort, :806-818);
+//      (:2100-2159), node starts (:2501-2532), nodes per level (:703-724),
+//      and the list of (start, split, end) symbol ranges of every node;
+//   3. a non-minimal alphabet is remapped to 0..sigma-1 (:170-227); a
+//      non-power-of-two alphabet also gets a histogram (its short codes
+//      make level sizes depend on symbol counts, :776-790);
+//   4. level 0 bits are packed from the text; then for every level l:
+//      RankSelect counts of level l; the node kernel computes rank0 at every
+//      node start of level l (precomputeRanksKernel, :332-352) and from it
+//      the count table C at each node's split point (zeros of a node =
+//      rank0(end) - rank0(start)), so no histogram pass is needed for
+//      power-of-two alphabets; the split kernel stably partitions every
+//      node of level l by its bit (the level l+1 order; the reference
+//      re-sorts the text on the top l+1 code bits, :806-818) and writes the
+//      bits of level l+1 directly;
 //   5. select samples of all levels.
-// Level order is carried as minimal symbols; the node of symbol c at level l
-// is found arithmetically for power-of-two alphabets and by the reference's
-// prevPow2 descent otherwise.  No kernel waits on another CTA.
+// The split kernel has a fast path for tiles that lie inside one node of a
+// power-of-two alphabet: warp ballots rank the tile's zeros and ones, both
+// go to two contiguous runs, and the next level's bits of each run are
+// compacted with warp OR-reductions into shared memory and stored as whole
+// words (only a run's two edge words use atomicOr).  Other tiles take a
+// general path that stages (destination, symbol) pairs in shared memory.
+// No kernel waits on another CTA.
 #include <algorithm>
 #include <cstring>
+#include <string>
 
 #include "internal.cuh"
 
@@ -96,6 +106,31 @@ std::vector<NodeInfoH> make_nodes(uint64_t sigma,
   return out;
 }
 
+// Every node with at least two symbols, level by level, in symbol order:
+// [start, end) splits at start + prevPow2(end - start), the descent of
+// deviceAccess (wavelet_tree.cuh:1854-1868).
+struct LevelNode {
+  uint64_t cs, split, end;
+};
+
+std::vector<std::vector<LevelNode>> make_level_nodes(uint64_t sigma,
+                                                     uint32_t L) {
+  std::vector<std::vector<LevelNode>> lv(L);
+  std::vector<std::pair<uint64_t, uint64_t>> cur{{0, sigma}}, nxt;
+  for (uint32_t l = 0; l < L; ++l) {
+    nxt.clear();
+    for (auto [a, e] : cur) {
+      if (e - a < 2) continue;
+      uint64_t const s = a + h_prev_pow2(e - a);
+      lv[l].push_back({a, s, e});
+      nxt.push_back({a, s});
+      nxt.push_back({s, e});
+    }
+    cur.swap(nxt);
+  }
+  return lv;
+}
+
 // --------------------------------------------------------------------------
 // Alphabet detection for 1- and 2-byte symbols: presence bitmap.
 template <class T>
@@ -117,52 +152,50 @@ __global__ void presence_kernel(T const* __restrict__ text, uint64_t n,
     if (sm[i]) atomicOr(&bitmap[i], sm[i]);
 }
 
-// --------------------------------------------------------------------------
-// Histogram (+ remap to minimal symbols when the alphabet is not 0..s-1).
-template <class T, bool IsMin>
+// Text -> minimal symbols (lower_bound in the sorted alphabet).
+template <class T>
 __global__ void __launch_bounds__(256)
-hist_kernel(T const* __restrict__ text, uint64_t n,
-            T const* __restrict__ alphabet, uint64_t sigma,
-            T* __restrict__ cur, unsigned long long* __restrict__ occ,
-            uint32_t* __restrict__ err, uint32_t smem_bins) {
-  extern __shared__ uint32_t hist[];  // smem_bins counters, or none
+remap_kernel(T const* __restrict__ text, uint64_t n,
+             T const* __restrict__ alphabet, uint64_t sigma,
+             T* __restrict__ cur, uint32_t* __restrict__ err) {
+  uint64_t const stride = uint64_t(gridDim.x) * blockDim.x;
+  uint32_t bad = 0;
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n;
+       i += stride) {
+    T const x = text[i];
+    uint64_t lo = 0, hi = sigma;
+    while (lo < hi) {
+      uint64_t const mid = (lo + hi) >> 1;
+      if (alphabet[mid] < x) lo = mid + 1; else hi = mid;
+    }
+    if (lo >= sigma) {
+      bad = 1;
+      lo = 0;
+    }
+    cur[i] = static_cast<T>(lo);
+  }
+  if (bad) atomicOr(err, 1u);
+}
+
+// Histogram of minimal symbols (non-power-of-two alphabets only).
+template <class T>
+__global__ void __launch_bounds__(256)
+hist_kernel(T const* __restrict__ text, uint64_t n, uint64_t sigma,
+            unsigned long long* __restrict__ occ, uint32_t smem_bins) {
+  extern __shared__ uint32_t hist[];
   bool const use_smem = smem_bins != 0;
   if (use_smem) {
     for (uint32_t i = threadIdx.x; i < smem_bins; i += blockDim.x) hist[i] = 0;
     __syncthreads();
   }
   uint64_t const stride = uint64_t(gridDim.x) * blockDim.x;
-  uint32_t bad = 0;
   for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n;
        i += stride) {
-    T const x = text[i];
-    uint64_t c;
-    if (IsMin) {
-      c = x;
-    } else {
-      uint64_t lo = 0, hi = sigma;
-      while (lo < hi) {
-        uint64_t const mid = (lo + hi) >> 1;
-        if (alphabet[mid] < x) lo = mid + 1; else hi = mid;
-      }
-      c = lo;
-    }
-    if (c >= sigma) {
-      bad = 1;
-      c = 0;
-    }
-    if (!IsMin) cur[i] = static_cast<T>(c);
-    if (use_smem) {
-      // Aggregate equal symbols of the warp into one shared atomic.
-      uint32_t const peers = __match_any_sync(__activemask(), uint32_t(c));
-      uint32_t const lane = threadIdx.x & 31;
-      if ((__ffs(peers) - 1) == int(lane))
-        atomicAdd(&hist[c], __popc(peers));
-    } else {
-      atomicAdd(&occ[c], 1ull);
-    }
+    uint64_t const c = text[i];
+    if (c >= sigma) continue;
+    if (use_smem) atomicAdd(&hist[c], 1u);
+    else atomicAdd(&occ[c], 1ull);
   }
-  if (bad) atomicOr(err, 1u);
   if (use_smem) {
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < smem_bins; i += blockDim.x)
@@ -199,16 +232,26 @@ __device__ __forceinline__ NodeRange node_of(uint64_t c, uint32_t l,
   return r;
 }
 
-// One thread per output word of level l: bit (c >= split) of 32 symbols.
-template <class T, bool Pow2>
+template <bool Pow2>
+__device__ __forceinline__ bool level_bit(uint64_t c, uint32_t l, uint32_t L,
+                                          uint64_t sigma) {
+  if (Pow2) return (c >> (L - 1 - l)) & 1;
+  return c >= node_of<false>(c, l, L, sigma).split;
+}
+
+// Level 0 bits: one thread per output word.  Check = validate symbols of a
+// minimal alphabet (c < sigma).
+template <class T, bool Pow2, bool Check>
 __global__ void __launch_bounds__(256)
-fill_level_kernel(T const* __restrict__ src, uint64_t size_l, uint32_t l,
-                  uint32_t L, uint64_t sigma, uint32_t* __restrict__ out) {
+fill0_kernel(T const* __restrict__ src, uint64_t size0, uint32_t L,
+             uint64_t sigma, uint32_t* __restrict__ out,
+             uint32_t* __restrict__ err) {
   uint64_t const w = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   uint64_t const p0 = w * 32;
-  if (p0 >= size_l) return;
+  if (p0 >= size0) return;
   uint32_t word = 0;
-  if (p0 + 32 <= size_l) {
+  bool bad = false;
+  if (p0 + 32 <= size0) {
     constexpr int kVec = 32 * sizeof(T) / 16;
     uint4 buf[kVec];
     uint4 const* s = reinterpret_cast<uint4 const*>(src + p0);
@@ -218,176 +261,55 @@ fill_level_kernel(T const* __restrict__ src, uint64_t size_l, uint32_t l,
 #pragma unroll
     for (int j = 0; j < 32; ++j) {
       uint64_t const c = e[j];
-      bool b;
-      if (Pow2) b = (c >> (L - 1 - l)) & 1;
-      else b = c >= node_of<false>(c, l, L, sigma).split;
-      word |= uint32_t(b) << j;
+      if (Check) bad |= c >= sigma;
+      word |= uint32_t(level_bit<Pow2>(c, 0, L, sigma)) << j;
     }
   } else {
-    for (uint32_t j = 0; p0 + j < size_l; ++j) {
+    for (uint32_t j = 0; p0 + j < size0; ++j) {
       uint64_t const c = src[p0 + j];
-      bool b;
-      if (Pow2) b = (c >> (L - 1 - l)) & 1;
-      else b = c >= node_of<false>(c, l, L, sigma).split;
-      word |= uint32_t(b) << j;
+      if (Check) bad |= c >= sigma;
+      word |= uint32_t(level_bit<Pow2>(c, 0, L, sigma)) << j;
     }
   }
   out[w] = word;
+  if (Check && bad) atomicOr(err, 1u);
 }
 
-// rank0 at each node start of level l (precomputeRanksKernel :332-352).
-__global__ void node_ranks_kernel(TreeView t, uint64_t const* __restrict__ starts,
-                                  uint64_t first, uint64_t count, uint32_t l,
-                                  uint64_t* __restrict__ ranks) {
+// For every node of level l with >= 2 symbols: rank0 at its start (stored
+// as the node-start rank of the reference) and the count table at its
+// split point, C[split] = C[start] + rank0(C[end]) - rank0(C[start]).
+__global__ void __launch_bounds__(128)
+level_nodes_kernel(TreeView t, LevelNode const* __restrict__ nodes,
+                   uint64_t count, uint32_t l, uint64_t* __restrict__ counts,
+                   uint64_t* __restrict__ ranks, uint32_t* __restrict__ err) {
   uint64_t const i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   if (i >= count) return;
+  LevelNode const nd = nodes[i];
   ArrayMeta const m = t.rs.meta[l];
-  uint64_t const pos = t.counts[starts[first + i]];
-  ranks[first + i] =
-      pos - ecl::detail::rs_rank1<false>(t.rs, m, pos, nullptr);
+  uint64_t const ps = counts[nd.cs];
+  uint64_t const pe = counts[nd.end];
+  uint64_t const r_start =
+      nd.cs ? ps - ecl::detail::rs_rank1<false>(t.rs, m, ps, nullptr) : 0;
+  uint64_t const r_end = pe - ecl::detail::rs_rank1<false>(t.rs, m, pe, nullptr);
+  counts[nd.split] = ps + (r_end - r_start);
+  if (nd.cs) {
+    uint64_t const ni = ecl::detail::node_index(t, t.node_base, nd.cs, l);
+    if (ni < t.num_ranks) ranks[ni] = r_start;
+    else atomicOr(err, 2u);
+  }
 }
 
-constexpr uint32_t kSplitThreads = 256;
-constexpr uint32_t kSplitItems = 16;
-constexpr uint32_t kSplitTile = kSplitThreads * kSplitItems;
+}  // namespace
+}  // namespace ewt
 
-// Stable partition of every node of level l by the level's bit: the symbol
-// at level position p (node [cs,ce], split s, zeros before p in the level Z)
-// moves to C[cs] + (Z - Zn) if c < s, else to C[s] + (p - C[cs]) - (Z - Zn),
-// where Zn = rank0 at the node start.  Positions >= size_l (symbols whose
-// code already ended) keep their place.  The tile stages (value, dest) in
-// shared memory in destination-run order so the global writes coalesce.
-template <class T, bool Pow2>
-__global__ void __launch_bounds__(kSplitThreads)
-split_level_kernel(T const* __restrict__ src, T* __restrict__ dst, uint64_t n,
-                   uint64_t size_l, uint32_t l, TreeView t,
-                   uint32_t* __restrict__ err) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  uint64_t* dests = reinterpret_cast<uint64_t*>(smem);
-  T* vals = reinterpret_cast<T*>(smem + kSplitTile * sizeof(uint64_t));
-  __shared__ uint32_t warp_z[kSplitThreads / 32];
+#include "split.cuh"
 
-  uint64_t const tile_start = blockIdx.x * uint64_t(kSplitTile);
-  uint64_t const tile_end = min(tile_start + kSplitTile, n);
-  uint32_t const tid = threadIdx.x;
-  ArrayMeta const m = t.rs.meta[l];
-  uint64_t const* counts = t.counts;
-  uint32_t const L = t.levels;
-
-  // Zeros of level l before the tile start (tile starts are 512-aligned).
-  uint64_t z_tile;
-  if (tile_start < size_l)
-    z_tile = tile_start - (t.rs.l1[m.l1_off + (tile_start >> 16)] +
-                           t.rs.l2[m.l2_off + (tile_start >> 9)]);
-  else
-    z_tile = m.bits - m.ones;
-
-  // Load this thread's 16 consecutive symbols.
-  uint64_t const p0 = tile_start + uint64_t(tid) * kSplitItems;
-  T item[kSplitItems];
-  if (p0 + kSplitItems <= n) {
-    constexpr int kVec = kSplitItems * sizeof(T) / 16;
-    uint4 buf[kVec];
-    uint4 const* s = reinterpret_cast<uint4 const*>(src + p0);
-#pragma unroll
-    for (int q = 0; q < kVec; ++q) buf[q] = __ldg(s + q);
-    T const* e = reinterpret_cast<T const*>(buf);
-#pragma unroll
-    for (int j = 0; j < int(kSplitItems); ++j) item[j] = e[j];
-  } else {
-#pragma unroll
-    for (int j = 0; j < int(kSplitItems); ++j)
-      item[j] = (p0 + j < n) ? src[p0 + j] : T(0);
-  }
-  uint32_t bits = 0, part = 0;
-#pragma unroll
-  for (int j = 0; j < int(kSplitItems); ++j) {
-    uint64_t const p = p0 + j;
-    if (p < size_l) {
-      part |= 1u << j;
-      uint64_t const c = item[j];
-      bool b;
-      if (Pow2) b = (c >> (L - 1 - l)) & 1;
-      else b = c >= node_of<false>(c, l, L, t.sigma).split;
-      bits |= uint32_t(b) << j;
-    }
-  }
-  uint32_t const zcnt = __popc(part & ~bits);
-  // CTA exclusive scan of zero counts.
-  uint32_t inc = zcnt;
-  uint32_t const lane = tid & 31, wid = tid >> 5;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    uint32_t const y = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= o) inc += y;
-  }
-  if (lane == 31) warp_z[wid] = inc;
-  __syncthreads();
-  uint32_t wbase = 0, tile_zeros = 0;
-#pragma unroll
-  for (uint32_t w = 0; w < kSplitThreads / 32; ++w) {
-    uint32_t const v = warp_z[w];
-    if (w < wid) wbase += v;
-    tile_zeros += v;
-  }
-  uint64_t zp = z_tile + wbase + inc - zcnt;
-
-#pragma unroll
-  for (int j = 0; j < int(kSplitItems); ++j) {
-    uint64_t const p = p0 + j;
-    if (p >= tile_end) break;
-    uint64_t slot, dest;
-    if ((part >> j) & 1) {
-      uint64_t const c = item[j];
-      bool const b = (bits >> j) & 1;
-      NodeRange const nr = node_of<Pow2>(c, l, L, t.sigma);
-      uint64_t const ca = counts[nr.cs];
-      uint64_t const cm = counts[nr.split];
-      uint64_t const cend = (nr.ce + 1 >= t.sigma) ? t.n : counts[nr.ce + 1];
-      uint64_t zn = 0;
-      if (nr.cs != 0) {
-        uint64_t const ni = ecl::detail::node_index(t, t.node_base, nr.cs, l);
-        if (ni < t.num_ranks) zn = t.node_ranks[ni];
-        else {
-          atomicOr(err, 2u);
-          atomicMin(err + 1, blockIdx.x);
-        }
-      }
-      uint64_t const f = max(ca, tile_start);
-      uint64_t const zf = ca > tile_start ? zn : z_tile;
-      uint64_t const ze =
-          cend <= tile_end ? zn + (cm - ca) : z_tile + tile_zeros;
-      uint64_t const zb = zp - zf;
-      slot = (f - tile_start) + (b ? (ze - zf) + (p - f - zb) : zb);
-      dest = b ? cm + (p - ca) - (zp - zn) : ca + (zp - zn);
-      if (!b) ++zp;
-    } else {
-      slot = p - tile_start;
-      dest = p;
-    }
-    // Consistency guard: a slot or destination outside the tile / text
-    // means corrupt bookkeeping; record it instead of writing out of range.
-    if (slot >= kSplitTile || dest >= n) {
-      atomicOr(err, slot >= kSplitTile ? 4u : 8u);
-      atomicMin(err + 1, blockIdx.x);
-      continue;
-    }
-    dests[slot] = dest;
-    vals[slot] = item[j];
-  }
-  __syncthreads();
-  uint32_t const cnt = static_cast<uint32_t>(tile_end - tile_start);
-  for (uint32_t s = tid; s < cnt; s += kSplitThreads) {
-    uint64_t const d = dests[s];
-    if (d < n) dst[d] = vals[s];
-  }
-}
+namespace ewt {
+namespace {
 
 template <class T>
 void build_typed(ewt_tree& t, const void* data, uint64_t n,
                  const void* alphabet, uint64_t sigma, cudaStream_t st) {
-  int const dev = t.device;
-  (void)dev;
   // ---- text on the device
   DevBuf text_owned;
   T const* d_text;
@@ -481,67 +403,70 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
     t.node_base[l] = t.node_base[l - 1] + t.nodes_at_level[l - 1];
   EWT_REQUIRE(t.node_base[L] == t.nodes.size(), EWT_ERR_UNSUPPORTED,
               "inconsistent node bookkeeping for this alphabet size");
-  for (size_t i = 0; i < t.nodes.size(); ++i) {
-    uint64_t const l = t.nodes[i].level;
-    EWT_REQUIRE(i >= t.node_base[l] && i < t.node_base[l + 1],
-                EWT_ERR_UNSUPPORTED, "node starts not grouped by level");
-  }
   t.nodes_until_last = L >= 1 ? t.node_base[L - 1] : 0;
+  auto const level_nodes = make_level_nodes(sigma, L);
 
   // ---- device tables
   t.err_d.alloc(16);
   EWT_CUDA(cudaMemsetAsync(t.err_d.get(), 0, 16, st));
-  EWT_CUDA(cudaMemsetAsync(t.err_d.as<uint32_t>() + 2, 0xFF, 4, st));
-  DevBuf cur_buf;  // remapped text when the alphabet is not 0..sigma-1
+  uint32_t* err_build = t.err_d.as<uint32_t>() + 1;
+  uint32_t const grid_stream =
+      static_cast<uint32_t>(std::min<uint64_t>(ceil_div(n, 256),
+                                               uint64_t(sm_count()) * 8));
+  DevBuf cur_buf;  // minimal symbols when the alphabet is not 0..sigma-1
+  T const* sym = d_text;
   if (!t.is_min) {
     std::vector<T> a(t.alphabet.begin(), t.alphabet.end());
     t.alphabet_d.alloc(sigma * sizeof(T));
     EWT_CUDA(cudaMemcpyAsync(t.alphabet_d.get(), a.data(), sigma * sizeof(T),
                              cudaMemcpyHostToDevice, st));
-    EWT_CUDA(cudaStreamSynchronize(st));
     cur_buf.alloc(n * sizeof(T));
-  }
-  DevBuf occ_d(sigma * 8);
-  EWT_CUDA(cudaMemsetAsync(occ_d.get(), 0, sigma * 8, st));
-  {
-    uint32_t const smem_bins = sigma <= 8192 ? static_cast<uint32_t>(sigma) : 0;
-    uint32_t const blocks = static_cast<uint32_t>(
-        std::min<uint64_t>(ceil_div(n, 256), uint64_t(sm_count()) * 8));
-    auto k = t.is_min ? hist_kernel<T, true> : hist_kernel<T, false>;
-    size_t const smem = smem_bins * 4;
-    if (smem > 48 * 1024)
-      EWT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    static_cast<int>(smem)));
     PhaseTimer pt(EWT_PHASE_HIST, st);
-    k<<<blocks, 256, smem, st>>>(d_text, n, t.alphabet_d.as<T>(), sigma,
-                                 cur_buf.as<T>(),
-                                 occ_d.as<unsigned long long>(),
-                                 t.err_d.as<uint32_t>(), smem_bins);
+    remap_kernel<T><<<grid_stream, 256, 0, st>>>(
+        d_text, n, t.alphabet_d.as<T>(), sigma, cur_buf.as<T>(), err_build);
     EWT_LAUNCHED();
+    sym = cur_buf.as<T>();
   }
-  t.occ.assign(sigma, 0);
-  uint32_t err = 0;
-  EWT_CUDA(cudaMemcpyAsync(t.occ.data(), occ_d.get(), sigma * 8,
-                           cudaMemcpyDeviceToHost, st));
-  EWT_CUDA(cudaMemcpyAsync(&err, t.err_d.get(), 4, cudaMemcpyDeviceToHost, st));
-  EWT_CUDA(cudaStreamSynchronize(st));
-  EWT_REQUIRE(err == 0, EWT_ERR_ALPHABET,
-              "the text holds a symbol above the alphabet's last symbol");
-  t.counts.assign(sigma, 0);
-  for (uint64_t c = 1; c < sigma; ++c) t.counts[c] = t.counts[c - 1] + t.occ[c - 1];
-  // Level sizes (wavelet_tree.cuh:776-790): drop symbols whose code ended.
+  // Count table: exact histogram for non-power-of-two alphabets (their level
+  // sizes need it); otherwise only C[0] = 0 and C[sigma] = n, the rest is
+  // derived level by level.
+  t.counts_d.alloc((sigma + 1) * 8);
   t.level_bits.assign(L, n);
-  for (uint32_t l = 0; l < L; ++l)
-    for (size_t j = 0; j < t.codes.size(); ++j)
-      if (t.codes[j].len <= l) t.level_bits[l] -= t.occ[t.codes_start + j];
+  if (!t.pow2) {
+    DevBuf occ_d(sigma * 8);
+    EWT_CUDA(cudaMemsetAsync(occ_d.get(), 0, sigma * 8, st));
+    uint32_t const smem_bins = sigma <= 8192 ? static_cast<uint32_t>(sigma) : 0;
+    {
+      PhaseTimer pt(EWT_PHASE_HIST, st);
+      hist_kernel<T><<<grid_stream, 256, smem_bins * 4, st>>>(
+          sym, n, sigma, occ_d.as<unsigned long long>(), smem_bins);
+      EWT_LAUNCHED();
+    }
+    t.occ.assign(sigma, 0);
+    EWT_CUDA(cudaMemcpyAsync(t.occ.data(), occ_d.get(), sigma * 8,
+                             cudaMemcpyDeviceToHost, st));
+    EWT_CUDA(cudaStreamSynchronize(st));
+    // Level sizes (wavelet_tree.cuh:776-790): drop symbols whose code ended.
+    for (uint32_t l = 0; l < L; ++l)
+      for (size_t j = 0; j < t.codes.size(); ++j)
+        if (t.codes[j].len <= l) t.level_bits[l] -= t.occ[t.codes_start + j];
+    std::vector<uint64_t> c(sigma + 1, 0);
+    for (uint64_t i = 1; i <= sigma; ++i) c[i] = c[i - 1] + t.occ[i - 1];
+    EWT_CUDA(cudaMemcpyAsync(t.counts_d.get(), c.data(), (sigma + 1) * 8,
+                             cudaMemcpyHostToDevice, st));
+  } else {
+    uint64_t const ends[2] = {0, n};
+    EWT_CUDA(cudaMemcpyAsync(t.counts_d.get(), &ends[0], 8,
+                             cudaMemcpyHostToDevice, st));
+    EWT_CUDA(cudaMemcpyAsync(t.counts_d.as<uint64_t>() + sigma, &ends[1], 8,
+                             cudaMemcpyHostToDevice, st));
+    EWT_CUDA(cudaStreamSynchronize(st));  // `ends` leaves scope
+  }
   for (uint32_t l = 0; l < L; ++l)
     EWT_REQUIRE(t.level_bits[l] > 0, EWT_ERR_UNSUPPORTED,
                 "empty level: every symbol with a code this long is absent");
 
   t.rs.layout(t.level_bits);
-  t.counts_d.alloc(sigma * 8);
-  EWT_CUDA(cudaMemcpyAsync(t.counts_d.get(), t.counts.data(), sigma * 8,
-                           cudaMemcpyHostToDevice, st));
   t.ranks_d.alloc(std::max<size_t>(t.nodes.size(), 1) * 8);
   t.node_base_d.alloc((L + 1) * 8);
   EWT_CUDA(cudaMemcpyAsync(t.node_base_d.get(), t.node_base.data(), (L + 1) * 8,
@@ -561,11 +486,17 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
                            cudaMemcpyHostToDevice, st));
   EWT_CUDA(cudaMemcpyAsync(t.code_bits_d.get(), cb.data(), nc * 8,
                            cudaMemcpyHostToDevice, st));
-  std::vector<uint64_t> starts(std::max<size_t>(t.nodes.size(), 1), 0);
-  for (size_t i = 0; i < t.nodes.size(); ++i) starts[i] = t.nodes[i].start;
-  DevBuf starts_d(starts.size() * 8);
-  EWT_CUDA(cudaMemcpyAsync(starts_d.get(), starts.data(), starts.size() * 8,
+  std::vector<LevelNode> flat;
+  std::vector<uint64_t> lv_off(L + 1, 0);
+  for (uint32_t l = 0; l < L; ++l) {
+    flat.insert(flat.end(), level_nodes[l].begin(), level_nodes[l].end());
+    lv_off[l + 1] = flat.size();
+  }
+  DevBuf lnodes_d(std::max<size_t>(flat.size(), 1) * sizeof(LevelNode));
+  EWT_CUDA(cudaMemcpyAsync(lnodes_d.get(), flat.data(),
+                           flat.size() * sizeof(LevelNode),
                            cudaMemcpyHostToDevice, st));
+  EWT_CUDA(cudaStreamSynchronize(st));  // host vectors above leave scope
 
   t.n = n;
   TreeView& v = t.view;
@@ -587,59 +518,73 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   v.is_pow2 = t.pow2;
   v.is_min = t.is_min;
 
-  // ---- levels
-  T const* src = t.is_min ? d_text : cur_buf.as<T>();
-  DevBuf ping, pong;
-  if (L > 1) ping.alloc(n * sizeof(T));
-  if (L > 2) pong.alloc(n * sizeof(T));
-  T* bufs[2] = {ping.as<T>(), pong.as<T>()};
-  size_t const split_smem = kSplitTile * (sizeof(uint64_t) + sizeof(T));
-  auto split_k = t.pow2 ? split_level_kernel<T, true> : split_level_kernel<T, false>;
-  EWT_CUDA(cudaFuncSetAttribute(split_k,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(split_smem)));
-  auto fill_k = t.pow2 ? fill_level_kernel<T, true> : fill_level_kernel<T, false>;
-  for (uint32_t l = 0; l < L; ++l) {
-    uint64_t const size_l = t.level_bits[l];
-    uint64_t const words = ceil_div(size_l, 32);
-    {
+  // ---- level 0 bits
+  uint32_t* const words = t.rs.words.as<uint32_t>();
+  {
     PhaseTimer pt(EWT_PHASE_FILL, st);
-    fill_k<<<static_cast<uint32_t>(ceil_div(words, 256)), 256, 0, st>>>(
-        src, size_l, l, L, sigma,
-        t.rs.words.as<uint32_t>() + t.rs.meta[l].word_off);
+    uint64_t const w0 = ceil_div(t.level_bits[0], 32);
+    uint32_t const blocks = static_cast<uint32_t>(ceil_div(w0, 256));
+    auto k = t.pow2 ? (t.is_min ? fill0_kernel<T, true, true>
+                                : fill0_kernel<T, true, false>)
+                    : (t.is_min ? fill0_kernel<T, false, true>
+                                : fill0_kernel<T, false, false>);
+    k<<<blocks, 256, 0, st>>>(sym, t.level_bits[0], L, sigma,
+                              words + t.rs.meta[0].word_off, err_build);
     EWT_LAUNCHED();
-    }
+  }
+  // ---- levels
+  DevBuf ping, pong;
+  if (L > 2) ping.alloc(n * sizeof(T));
+  if (L > 3) pong.alloc(n * sizeof(T));
+  T* bufs[2] = {ping.as<T>(), pong.as<T>()};
+  DevBuf slow_tiles(ceil_div(n, kSplitTile));  // per-tile flags of the split
+  T const* src = sym;
+  for (uint32_t l = 0; l < L; ++l) {
     build_rs_counts(t.rs, l, l + 1, st);
-    uint64_t const nfirst = t.node_base[l], ncount = t.node_base[l + 1] - nfirst;
+    uint64_t const ncount = lv_off[l + 1] - lv_off[l];
     if (ncount > 0) {
       PhaseTimer pt(EWT_PHASE_NODE_RANKS, st);
-      node_ranks_kernel<<<static_cast<uint32_t>(ceil_div(ncount, 128)), 128, 0,
-                          st>>>(v, starts_d.as<uint64_t>(), nfirst, ncount, l,
-                                t.ranks_d.as<uint64_t>());
+      level_nodes_kernel<<<static_cast<uint32_t>(ceil_div(ncount, 128)), 128,
+                           0, st>>>(v, lnodes_d.as<LevelNode>() + lv_off[l],
+                                    ncount, l, t.counts_d.as<uint64_t>(),
+                                    t.ranks_d.as<uint64_t>(), err_build);
       EWT_LAUNCHED();
     }
     if (l + 1 < L) {
-      T* dst = bufs[l & 1];
+      ArrayMeta const& mn = t.rs.meta[l + 1];
+      EWT_CUDA(cudaMemsetAsync(words + mn.word_off, 0,
+                               ceil_div(mn.bits, 32) * 4, st));
+      bool const write_order = l + 2 < L;
+      T* dst = write_order ? bufs[l & 1] : nullptr;
       PhaseTimer pt(EWT_PHASE_SPLIT, st);
-      split_k<<<static_cast<uint32_t>(ceil_div(n, kSplitTile)), kSplitThreads,
-                split_smem, st>>>(src, dst, n, size_l, l, v,
-                                  t.err_d.as<uint32_t>() + 1);
-      EWT_LAUNCHED();
+      if (t.pow2)
+        launch_split<T, true>(write_order, src, dst, n, t.level_bits[l],
+                              mn.bits, l, v, words + mn.word_off,
+                              slow_tiles.as<uint8_t>(), err_build, st);
+      else
+        launch_split<T, false>(write_order, src, dst, n, t.level_bits[l],
+                               mn.bits, l, v, words + mn.word_off,
+                               slow_tiles.as<uint8_t>(), err_build, st);
       src = dst;
-      uint32_t build_err[2] = {0, 0};
-      EWT_CUDA(cudaMemcpyAsync(build_err, t.err_d.as<uint32_t>() + 1, 8,
-                               cudaMemcpyDeviceToHost, st));
-      EWT_CUDA(cudaStreamSynchronize(st));
-      EWT_REQUIRE(build_err[0] == 0, EWT_ERR_CUDA,
-                  "internal consistency check failed while partitioning "
-                  "level " + std::to_string(l) + " (kind " +
-                      std::to_string(build_err[0]) + ", first tile " +
-                      std::to_string(build_err[1]) + ")");
     }
   }
   build_rs_samples(t.rs, st);
   v.rs = t.rs.view();
+  uint32_t build_err = 0;
+  EWT_CUDA(cudaMemcpyAsync(&build_err, err_build, 4, cudaMemcpyDeviceToHost,
+                           st));
+  std::vector<uint64_t> c(sigma + 1);
+  EWT_CUDA(cudaMemcpyAsync(c.data(), t.counts_d.get(), (sigma + 1) * 8,
+                           cudaMemcpyDeviceToHost, st));
   EWT_CUDA(cudaStreamSynchronize(st));
+  EWT_REQUIRE(!(build_err & 1), EWT_ERR_ALPHABET,
+              "the text holds a symbol above the alphabet's last symbol");
+  EWT_REQUIRE(build_err == 0, EWT_ERR_CUDA,
+              "internal consistency check failed while building levels (kind " +
+                  std::to_string(build_err) + ")");
+  t.counts.assign(c.begin(), c.begin() + sigma);
+  t.occ.resize(sigma);
+  for (uint64_t i = 0; i < sigma; ++i) t.occ[i] = c[i + 1] - c[i];
 }
 
 }  // namespace
