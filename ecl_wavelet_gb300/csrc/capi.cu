@@ -472,6 +472,7 @@ int ewt_rs_build(const uint32_t* words, const uint64_t* bits,
     EWT_LAUNCHED();
     build_rs_counts(r->rs, 0, num_arrays, r->stream);
     build_rs_samples(r->rs, r->stream);
+    build_rank_blocks(r->rs, r->stream);
     *out = r.release();
   });
 }

@@ -19,7 +19,7 @@ using ecl::detail::TreeView;
 // do: arrays padded to 32-word multiples, total word count even.
 struct RSStore {
   std::vector<ArrayMeta> meta;  // host copy
-  DevBuf words, l1, l2, s0, s1, meta_d, jobs_d;
+  DevBuf words, l1, l2, s0, s1, meta_d, jobs_d, rb;
   uint64_t total_words = 0, total_l1 = 0, total_l2 = 0;
   uint64_t total_s0 = 0, total_s1 = 0;
 
@@ -28,7 +28,7 @@ struct RSStore {
   void layout(std::vector<uint64_t> const& bits);
   RSView view() const;
   uint64_t device_bytes() const {
-    return words.bytes() + l1.bytes() + l2.bytes() + s0.bytes() + s1.bytes() +
+    return words.bytes() + l1.bytes() + l2.bytes() + s0.bytes() + s1.bytes() + rb.bytes() +
            meta_d.bytes();
   }
 };
@@ -41,6 +41,9 @@ void build_rs_counts(RSStore& rs, uint32_t first, uint32_t last,
 // Allocates and fills the select samples of every array (needs counts of
 // all arrays) and uploads the final meta table.
 void build_rs_samples(RSStore& rs, cudaStream_t stream);
+// Builds the query-side rank blocks of every array (needs the counts) and
+// uploads the meta table with their offsets.
+void build_rank_blocks(RSStore& rs, cudaStream_t stream);
 
 struct QueryScratch {
   DevBuf in, out, types;

@@ -137,6 +137,110 @@ query_kernel(TreeView t, uint8_t const* __restrict__ types,
   if (bad) atomicOr(err, 1u);
 }
 
+// Batched mixed form: CTAs take 2048-query chunks of the interleaved batch,
+// sort each chunk's query numbers by type in shared memory (warp ballots),
+// then walk the access, rank and select lists in turn, so every warp runs
+// one kind of walk.  Results go straight to their original slots.
+constexpr uint32_t kMixChunk = 2048;
+
+template <class T>
+__global__ void __launch_bounds__(kQueryThreads)
+mixed_kernel(TreeView t, uint8_t const* __restrict__ types,
+             QueryRec<T> const* __restrict__ in, uint64_t m,
+             uint64_t* __restrict__ out, uint32_t* __restrict__ err,
+             uint32_t stage_counts, uint32_t stage_ranks) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint16_t lists[3][kMixChunk];
+  __shared__ uint32_t list_len[3];
+  uint32_t const L = t.levels;
+  ArrayMeta* meta = reinterpret_cast<ArrayMeta*>(smem);
+  uint64_t* node_base = reinterpret_cast<uint64_t*>(meta + L);
+  size_t off = L * sizeof(ArrayMeta) + (L + 1) * 8;
+  off = (off + 15) & ~size_t(15);
+  uint64_t const* counts = t.counts;
+  uint64_t const* ranks = t.node_ranks;
+  {
+    uint64_t const* gm = reinterpret_cast<uint64_t const*>(t.rs.meta);
+    uint64_t* sm = reinterpret_cast<uint64_t*>(meta);
+    uint32_t const mw = L * (sizeof(ArrayMeta) / 8);
+    for (uint32_t i = threadIdx.x; i < mw; i += blockDim.x) sm[i] = gm[i];
+    for (uint32_t i = threadIdx.x; i <= L; i += blockDim.x)
+      node_base[i] = t.node_base[i];
+    if (stage_counts) {
+      uint64_t* sc = reinterpret_cast<uint64_t*>(smem + off);
+      for (uint64_t i = threadIdx.x; i < t.sigma; i += blockDim.x)
+        sc[i] = t.counts[i];
+      counts = sc;
+      off += t.sigma * 8;
+    }
+    if (stage_ranks) {
+      uint64_t* sr = reinterpret_cast<uint64_t*>(smem + off);
+      for (uint64_t i = threadIdx.x; i < t.num_ranks; i += blockDim.x)
+        sr[i] = t.node_ranks[i];
+      ranks = sr;
+    }
+  }
+  uint32_t const lane = threadIdx.x & 31;
+  uint32_t const lt = (1u << lane) - 1u;
+  uint32_t bad = 0;
+  uint64_t const chunks = (m + kMixChunk - 1) / kMixChunk;
+  for (uint64_t c = blockIdx.x; c < chunks; c += gridDim.x) {
+    uint64_t const base = c * kMixChunk;
+    if (threadIdx.x < 3) list_len[threadIdx.x] = 0;
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < kMixChunk; j += blockDim.x) {
+      uint64_t const q = base + j;
+      uint32_t const ty = q < m ? types[q] : 3u;
+#pragma unroll
+      for (uint32_t k = 0; k < 3; ++k) {
+        uint32_t const mask = __ballot_sync(0xffffffffu, ty == k);
+        if (mask == 0) continue;
+        uint32_t pos = 0;
+        if (lane == __ffs(mask) - 1) pos = atomicAdd(&list_len[k], __popc(mask));
+        pos = __shfl_sync(0xffffffffu, pos, __ffs(mask) - 1);
+        if (ty == k) lists[k][pos + __popc(mask & lt)] = static_cast<uint16_t>(j);
+      }
+      if (ty > 2 && q < m) {
+        out[q] = UINT64_MAX;
+        bad = 1;
+      }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < list_len[0]; i += blockDim.x) {
+      uint64_t const q = base + lists[0][i];
+      uint64_t const idx = in[q].index;
+      out[q] = idx < t.n ? static_cast<uint64_t>(from_minimal<T>(
+                               t, wt_access(t, meta, counts, ranks, node_base,
+                                            idx)))
+                         : 0;
+    }
+    for (uint32_t i = threadIdx.x; i < list_len[1]; i += blockDim.x) {
+      uint64_t const q = base + lists[1][i];
+      QueryRec<T> const r = in[q];
+      uint64_t const sym = to_minimal<T>(t, r.symbol);
+      if (sym >= t.sigma || r.index > t.n) {
+        out[q] = UINT64_MAX;
+        bad = 1;
+      } else {
+        out[q] = wt_rank(t, meta, counts, ranks, node_base, sym, r.index);
+      }
+    }
+    for (uint32_t i = threadIdx.x; i < list_len[2]; i += blockDim.x) {
+      uint64_t const q = base + lists[2][i];
+      QueryRec<T> const r = in[q];
+      uint64_t const sym = to_minimal<T>(t, r.symbol);
+      if (sym >= t.sigma || r.index == 0) {
+        out[q] = UINT64_MAX;
+        bad = 1;
+      } else {
+        out[q] = wt_select(t, meta, counts, ranks, node_base, sym, r.index);
+      }
+    }
+    __syncthreads();  // lists are reused by the next chunk
+  }
+  if (bad) atomicOr(err, 1u);
+}
+
 template <int Value>
 __global__ void __launch_bounds__(256)
 rs_rank_kernel(RSView v, uint32_t array, uint64_t const* __restrict__ pos,
@@ -188,6 +292,31 @@ void launch_typed(ewt_tree& t, uint8_t const* types, void const* in,
               EWT_ERR_INVALID_ARGUMENT,
               "query and result buffers must be 8-byte aligned");
   StagePlan const p = plan_stage(t);
+  if (K == kMixed) {
+    auto mk = mixed_kernel<T>;
+    static thread_local bool mattr[4] = {};
+    int const mi = sizeof(T) == 1 ? 0 : sizeof(T) == 2 ? 1 : sizeof(T) == 4 ? 2 : 3;
+    if (!mattr[mi]) {
+      EWT_CUDA(cudaFuncSetAttribute(
+          mk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+          static_cast<int>(kStageLimitBytes + 4096)));
+      mattr[mi] = true;
+    }
+    int per_sm = 0;
+    EWT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mk,
+                                                           kQueryThreads, p.bytes));
+    per_sm = std::max(per_sm, 1);
+    uint64_t const chunks = ceil_div(m, kMixChunk);
+    uint32_t const blocks = static_cast<uint32_t>(
+        std::min<uint64_t>(chunks, uint64_t(per_sm) * sm_count()));
+    PhaseTimer pt(EWT_PHASE_QUERY, s);
+    mk<<<blocks, kQueryThreads, p.bytes, s>>>(
+        t.view, types, static_cast<QueryRec<T> const*>(in), m,
+        static_cast<uint64_t*>(out), t.err_d.as<uint32_t>(), p.stage_counts,
+        p.stage_ranks);
+    EWT_LAUNCHED();
+    return;
+  }
   auto k = query_kernel<T, K>;
   static thread_local bool attr_set[4][4] = {};
   int const ti = sizeof(T) == 1 ? 0 : sizeof(T) == 2 ? 1 : sizeof(T) == 4 ? 2 : 3;

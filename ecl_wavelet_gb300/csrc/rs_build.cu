@@ -77,6 +77,7 @@ RSView RSStore::view() const {
   v.s0 = s0.as<uint64_t>();
   v.s1 = s1.as<uint64_t>();
   v.meta = meta_d.as<ArrayMeta>();
+  v.rb = rb.get() ? rb.as<uint4>() : nullptr;
   v.num_arrays = static_cast<uint32_t>(meta.size());
   return v;
 }
@@ -309,6 +310,68 @@ void build_rs_samples(RSStore& rs, cudaStream_t stream) {
   } else {
     EWT_CUDA(cudaStreamSynchronize(stream));
   }
+}
+
+namespace {
+
+// One thread per rank block (64-byte line) of every array: the number of
+// ones before the block (from the L1/L2 counts) and the block's 14 words.
+__global__ void __launch_bounds__(256)
+rank_blocks_kernel(RSView v, uint64_t const* __restrict__ line_start,
+                   uint32_t num_arrays, uint64_t total_lines,
+                   uint64_t total_words, uint4* __restrict__ out) {
+  uint64_t const g = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (g >= total_lines) return;
+  uint32_t lo = 0, hi = num_arrays - 1;
+  while (lo < hi) {
+    uint32_t const mid = (lo + hi + 1) >> 1;
+    if (line_start[mid] <= g) lo = mid; else hi = mid - 1;
+  }
+  ArrayMeta const m = v.meta[lo];
+  uint64_t const b = g - line_start[lo];
+  uint64_t const pos = b * ecl::detail::kRankBlockBits;
+  uint64_t const ones = ecl::detail::rs_rank1<false>(v, m, pos, nullptr);
+  uint64_t const w0 = m.word_off + b * ecl::detail::kRankBlockWords;
+  uint32_t w[ecl::detail::kRankBlockWords];
+#pragma unroll
+  for (uint32_t j = 0; j < ecl::detail::kRankBlockWords; ++j)
+    w[j] = w0 + j < total_words ? v.words[w0 + j] : 0u;
+  uint4* line = out + g * 4;
+  line[0] = make_uint4(static_cast<uint32_t>(ones),
+                       static_cast<uint32_t>(ones >> 32), w[0], w[1]);
+  line[1] = make_uint4(w[2], w[3], w[4], w[5]);
+  line[2] = make_uint4(w[6], w[7], w[8], w[9]);
+  line[3] = make_uint4(w[10], w[11], w[12], w[13]);
+}
+
+}  // namespace
+
+void build_rank_blocks(RSStore& rs, cudaStream_t stream) {
+  uint32_t const count = static_cast<uint32_t>(rs.meta.size());
+  std::vector<uint64_t> start(count);
+  uint64_t total = 0;
+  for (uint32_t a = 0; a < count; ++a) {
+    rs.meta[a].rb_off = total;
+    start[a] = total;
+    total += ceil_div(rs.meta[a].bits, ecl::detail::kRankBlockBits);
+  }
+  rs.rb.alloc(total * 64);
+  DevBuf start_d(count * 8);
+  EWT_CUDA(cudaMemcpyAsync(start_d.get(), start.data(), count * 8,
+                           cudaMemcpyHostToDevice, stream));
+  EWT_CUDA(cudaMemcpyAsync(rs.meta_d.get(), rs.meta.data(),
+                           count * sizeof(ArrayMeta), cudaMemcpyHostToDevice,
+                           stream));
+  RSView v = rs.view();
+  v.rb = nullptr;  // headers come from the L1/L2 counts
+  {
+    PhaseTimer pt(EWT_PHASE_SAMPLES, stream);
+    rank_blocks_kernel<<<static_cast<uint32_t>(ceil_div(total, 256)), 256, 0,
+                         stream>>>(v, start_d.as<uint64_t>(), count, total,
+                                   rs.total_words, rs.rb.as<uint4>());
+    EWT_LAUNCHED();
+  }
+  EWT_CUDA(cudaStreamSynchronize(stream));
 }
 
 }  // namespace ewt

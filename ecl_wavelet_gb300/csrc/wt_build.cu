@@ -569,6 +569,7 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
     }
   }
   build_rs_samples(t.rs, st);
+  build_rank_blocks(t.rs, st);
   v.rs = t.rs.view();
   uint32_t build_err = 0;
   EWT_CUDA(cudaMemcpyAsync(&build_err, err_build, 4, cudaMemcpyDeviceToHost,

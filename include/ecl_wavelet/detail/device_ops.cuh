@@ -43,7 +43,15 @@ struct ArrayMeta {
   uint64_t ones;        // total number of ones
   uint64_t num_l1;      // number of L1 blocks
   uint64_t num_last_l2; // L2 blocks inside the last L1 block
+  uint64_t rb_off;      // first rank block (64-byte line) of the array
 };
+
+/* Query-side rank blocks: each 64-byte line holds the number of ones before
+ * its first bit (uint64) followed by 448 bits of the array, so a rank reads
+ * one line.  An auxiliary copy next to the reference-format arrays, which
+ * stay the source of truth for exports and select. */
+constexpr uint64_t kRankBlockBits = 448;
+constexpr uint64_t kRankBlockWords = kRankBlockBits / 32;
 
 /* A set of bit arrays with rank/select support, all in device memory. */
 struct RSView {
@@ -53,6 +61,7 @@ struct RSView {
   const uint64_t* s0;
   const uint64_t* s1;
   const ArrayMeta* meta;  // device array of num_arrays entries
+  const uint4* rb;        // rank blocks (4 uint4 per line), may be null
   uint32_t num_arrays;
   uint32_t reserved;
 };
@@ -124,6 +133,32 @@ __device__ __forceinline__ uint64_t rs_rank1(const RSView& v,
   if (pos >= m.bits) {
     if (GetBit) *bit = false;
     return m.ones;
+  }
+  if (v.rb) {
+    // One 64-byte line: ones before the block + 14 data words.
+    uint64_t const blk = pos / kRankBlockBits;
+    uint32_t const off = static_cast<uint32_t>(pos - blk * kRankBlockBits);
+    uint4 const* line = v.rb + (m.rb_off + blk) * 4;
+    uint32_t const wi = off >> 5;
+    uint4 const q0 = __ldg(line);
+    uint4 const q1 = __ldg(line + 1);
+    uint4 q2 = make_uint4(0, 0, 0, 0), q3 = q2;
+    if (wi >= 6) {
+      q2 = __ldg(line + 2);
+      q3 = __ldg(line + 3);
+    }
+    uint32_t const w[kRankBlockWords] = {q0.z, q0.w, q1.x, q1.y, q1.z,
+                                         q1.w, q2.x, q2.y, q2.z, q2.w,
+                                         q3.x, q3.y, q3.z, q3.w};
+    uint32_t acc = 0, cur = 0;
+#pragma unroll
+    for (uint32_t j = 0; j < kRankBlockWords; ++j) {
+      acc += j < wi ? __popc(w[j]) : 0u;
+      cur = j == wi ? w[j] : cur;
+    }
+    acc += __popc(cur & ((1u << (off & 31)) - 1u));
+    if (GetBit) *bit = (cur >> (off & 31)) & 1u;
+    return ((uint64_t(q0.y) << 32) | q0.x) + acc;
   }
   uint64_t const b2 = pos >> 9;
   uint64_t r = __ldg(v.l1 + m.l1_off + (pos >> 16));
