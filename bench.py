@@ -49,6 +49,9 @@ def parse():
     p.add_argument("--no-sweep", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-sample", type=int, default=1 << 25)
+    p.add_argument("--only", default="all", choices=["all", "build", "queries"],
+                   help="build: stop after the timed builds; queries: also "
+                        "time the query batches (for profiling runs)")
     return p.parse_args()
 
 
@@ -287,8 +290,14 @@ def run_ours(args, world, rank, local):
              "compulsory_frac_of_peak": (compulsory / (step_ms / 1e3) / 1e9)
              / peak}
 
+    queries, e2e, sweep, cpu = {}, None, {}, None
+    if args.only == "build":
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "GB/s",
+                              "ms_per_step": step_ms, "roofline": roofline,
+                              "build": build, "partial": "build only"}))
+        return
     # ---- queries on the last tree -----------------------------------------
-    queries = {}
     m = args.queries
     qgen = torch.Generator(device=dev).manual_seed(77 + rank)
     types, rec = make_mixed_queries(torch, tree, n, sigma, m, qgen)
@@ -355,6 +364,11 @@ def run_ours(args, world, rank, local):
                "select": sel_ms, "e2e_mixed": e2e_q_ms},
     }
     del out, o_acc, o_r, o_s, rq, sq, acc_idx, rec, types
+    if args.only == "queries":
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value,
+                              "queries": queries, "partial": "build+queries"}))
+        return
 
     # ---- end-to-end build from pinned host memory --------------------------
     h_text = torch.empty(n, dtype=torch.uint8).pin_memory()
@@ -379,7 +393,6 @@ def run_ours(args, world, rank, local):
     del h_text, h_np
 
     # ---- sigma sweep -------------------------------------------------------
-    sweep = {}
     if not args.no_sweep:
         for s in (4, 16, 64, 256):
             if s == sigma:
@@ -396,7 +409,6 @@ def run_ours(args, world, rank, local):
             del t2
 
     # ---- CPU baseline (rank 0, N = 1 only) ---------------------------------
-    cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         from oracle import oracle as O
         sample = args.cpu_sample

@@ -50,15 +50,19 @@ template <class T, bool Pow2, bool WriteOrder>
 __global__ void __launch_bounds__(kSplitThreads, 3)
 split_kernel(T const* __restrict__ src, T* __restrict__ dst, uint64_t n,
              uint64_t size_l, uint64_t size_next, uint32_t l, TreeView t,
-             uint32_t* __restrict__ next, uint8_t const* __restrict__ slow,
+             uint32_t* __restrict__ next, uint32_t const* __restrict__ list,
+             uint32_t const* __restrict__ list_len,
              uint32_t* __restrict__ err) {
-  // Tiles the fast kernel already handled have slow[tile] == 0 (the text's
-  // last, partial tile is never handled there).
-  if (slow && blockIdx.x < n / kSplitTile && !slow[blockIdx.x]) return;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t warp_z[kSplitWarps];
-
-  uint64_t const tile_start = blockIdx.x * uint64_t(kSplitTile);
+  // Work items: every tile, or (after the fast kernel) the tiles it listed
+  // plus the text's last tile when that one is partial.
+  uint64_t const tiles = (n + kSplitTile - 1) / kSplitTile;
+  uint64_t const listed = list ? *list_len : 0;
+  uint64_t const items = list ? listed + (n % kSplitTile ? 1 : 0) : tiles;
+  for (uint64_t wi = blockIdx.x; wi < items; wi += gridDim.x) {
+  uint64_t const tile = !list ? wi : (wi < listed ? list[wi] : tiles - 1);
+  uint64_t const tile_start = tile * uint64_t(kSplitTile);
   uint64_t const tile_end = min(tile_start + kSplitTile, n);
   uint32_t const cnt = static_cast<uint32_t>(tile_end - tile_start);
   uint32_t const tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -165,6 +169,8 @@ split_kernel(T const* __restrict__ src, T* __restrict__ dst, uint64_t n,
       uint64_t const d = dests[s];
       if (d < n) dst[d] = vals[s];
     }
+  }
+  __syncthreads();  // shared memory is reused by the next item
   }
 }
 
@@ -292,14 +298,14 @@ __device__ __forceinline__ uint32_t pack_bits32(T const* run, uint32_t b) {
 //   4. the staged runs go to the new order with funnel-shifted word stores
 //      and their level l+1 bits are packed from the staged symbols and
 //      written as whole words (atomicOr only on a run's two edge words).
-// A tile whose symbols span two nodes is flagged in `slow` for the general
-// kernel.
+// A tile whose symbols span two nodes is appended to `slow_list` for the
+// general kernel.
 template <class T, bool WriteOrder>
 __global__ void __launch_bounds__(kSplitThreads, 3)
 split_fast_kernel(T const* __restrict__ src, T* __restrict__ dst, uint64_t n,
                   uint32_t l, TreeView t, uint32_t* __restrict__ next,
-                  uint64_t next_words, uint8_t* __restrict__ slow,
-                  uint32_t* __restrict__ err) {
+                  uint64_t next_words, uint32_t* __restrict__ slow_list,
+                  uint32_t* __restrict__ slow_len, uint32_t* __restrict__ err) {
   constexpr uint32_t kStages = split_stages<T>();
   constexpr uint32_t kTileBytes = kSplitTile * sizeof(T);
   constexpr uint32_t kStageBytes = split_stage_bytes<T>();
@@ -453,7 +459,7 @@ split_fast_kernel(T const* __restrict__ src, T* __restrict__ dst, uint64_t n,
       store_run(next, next_words, d0, nz, zwords);
       store_run(next, next_words, d1, no, owords);
     } else if (tid == 0) {
-      slow[tile] = 1;
+      slow_list[atomicAdd(slow_len, 1u)] = static_cast<uint32_t>(tile);
     }
     __syncthreads();  // stage, words and ring stage s are free again
     if (tid == 0 && k + kStages < mine) {
@@ -467,14 +473,15 @@ split_fast_kernel(T const* __restrict__ src, T* __restrict__ dst, uint64_t n,
 template <class T, bool Pow2>
 void launch_split(bool write_order, T const* src, T* dst, uint64_t n,
                   uint64_t size_l, uint64_t size_next, uint32_t l,
-                  TreeView const& v, uint32_t* next, uint8_t* slow,
+                  TreeView const& v, uint32_t* next, uint32_t* slow_list,
                   uint32_t* err, cudaStream_t st) {
   uint64_t const tiles = ceil_div(n, kSplitTile);
   // The fast kernel covers full tiles of a power-of-two alphabet (all of
   // them participate: size_l == n); the general kernel finishes the rest.
   bool const use_fast = Pow2 && size_l == n && n >= kSplitTile;
+  uint32_t* slow_len = slow_list + tiles;
   if (use_fast) {
-    EWT_CUDA(cudaMemsetAsync(slow, 0, tiles, st));
+    EWT_CUDA(cudaMemsetAsync(slow_len, 0, 4, st));
     size_t const ring = size_t(split_stages<T>()) * kSplitTile * sizeof(T) +
                         split_stage_bytes<T>();
     auto fk = write_order ? split_fast_kernel<T, true>
@@ -485,7 +492,8 @@ void launch_split(bool write_order, T const* src, T* dst, uint64_t n,
     uint32_t const grid = static_cast<uint32_t>(
         std::min<uint64_t>(n / kSplitTile, uint64_t(sm_count()) * 3));
     fk<<<grid, kSplitThreads, ring, st>>>(src, dst, n, l, v, next,
-                                          ceil_div(size_next, 32), slow, err);
+                                          ceil_div(size_next, 32), slow_list,
+                                          slow_len, err);
     EWT_LAUNCHED();
   }
   size_t const smem = kSplitTile * (sizeof(uint64_t) + sizeof(T));
@@ -493,12 +501,13 @@ void launch_split(bool write_order, T const* src, T* dst, uint64_t n,
                        : split_kernel<T, Pow2, false>;
   EWT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 static_cast<int>(smem)));
-  k<<<static_cast<uint32_t>(tiles), kSplitThreads, smem, st>>>(
-      src, dst, n, size_l, size_next, l, v, next, use_fast ? slow : nullptr,
-      err);
+  uint32_t const grid = static_cast<uint32_t>(
+      std::min<uint64_t>(tiles, uint64_t(sm_count()) * 3));
+  k<<<grid, kSplitThreads, smem, st>>>(src, dst, n, size_l, size_next, l, v,
+                                       next, use_fast ? slow_list : nullptr,
+                                       use_fast ? slow_len : nullptr, err);
   EWT_LAUNCHED();
 }
-
 
 }  // namespace
 }  // namespace ewt

@@ -537,7 +537,8 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   if (L > 2) ping.alloc(n * sizeof(T));
   if (L > 3) pong.alloc(n * sizeof(T));
   T* bufs[2] = {ping.as<T>(), pong.as<T>()};
-  DevBuf slow_tiles(ceil_div(n, kSplitTile));  // per-tile flags of the split
+  // tiles the fast split leaves to the general one, and their count
+  DevBuf slow_tiles((ceil_div(n, kSplitTile) + 1) * 4);
   T const* src = sym;
   for (uint32_t l = 0; l < L; ++l) {
     build_rs_counts(t.rs, l, l + 1, st);
@@ -560,11 +561,11 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
       if (t.pow2)
         launch_split<T, true>(write_order, src, dst, n, t.level_bits[l],
                               mn.bits, l, v, words + mn.word_off,
-                              slow_tiles.as<uint8_t>(), err_build, st);
+                              slow_tiles.as<uint32_t>(), err_build, st);
       else
         launch_split<T, false>(write_order, src, dst, n, t.level_bits[l],
                                mn.bits, l, v, words + mn.word_off,
-                               slow_tiles.as<uint8_t>(), err_build, st);
+                               slow_tiles.as<uint32_t>(), err_build, st);
       src = dst;
     }
   }
