@@ -98,6 +98,8 @@ SIGNATURES = {
     "ewt_mixed_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_uint64, C.c_void_p, C.c_void_p]),
     "ewt_query_status": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ewt_mixed_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_uint64, C.c_void_p]),
     "ewt_get_device_view": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "ewt_rs_build": (C.c_int, [C.c_void_p, _U64P, C.c_uint32, C.c_int,
                                C.POINTER(C.c_void_p)]),

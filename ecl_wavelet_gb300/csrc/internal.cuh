@@ -106,6 +106,11 @@ void launch_select(ewt_tree& t, const void* d_q, uint64_t m, uint64_t* d_out,
                    cudaStream_t s);
 void launch_mixed(ewt_tree& t, const uint8_t* d_types, const void* d_q,
                   uint64_t m, uint64_t* d_out, cudaStream_t s);
+// The mixed kernel over caller-provided device buffers with an explicit
+// invalid-query word; allocates nothing and records no timing events.
+void launch_mixed_raw(ewt_tree& t, const uint8_t* d_types, const void* d_q,
+                      uint64_t m, uint64_t* d_out, uint32_t* d_err,
+                      cudaStream_t s);
 void launch_rs_rank(ewt_rs& r, int array, int value, const uint64_t* d_pos,
                     uint64_t m, uint64_t* d_out, cudaStream_t s);
 void launch_rs_select(ewt_rs& r, int array, int value, const uint64_t* d_i,

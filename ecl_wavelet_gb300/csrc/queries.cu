@@ -375,6 +375,40 @@ void launch_mixed(ewt_tree& t, uint8_t const* d_types, void const* d_q,
   launch_any<kMixed>(t, d_types, d_q, m, d_out, s);
 }
 
+namespace {
+template <class T>
+void launch_mixed_raw_typed(ewt_tree& t, uint8_t const* d_types,
+                            void const* d_q, uint64_t m, uint64_t* d_out,
+                            uint32_t* d_err, cudaStream_t s) {
+  StagePlan const p = plan_stage(t);
+  auto mk = mixed_kernel<T>;
+  EWT_CUDA(cudaFuncSetAttribute(mk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(kStageLimitBytes + 4096)));
+  int per_sm = 0;
+  EWT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mk,
+                                                         kQueryThreads, p.bytes));
+  per_sm = std::max(per_sm, 1);
+  uint32_t const blocks = static_cast<uint32_t>(std::min<uint64_t>(
+      ceil_div(m, kMixChunk), uint64_t(per_sm) * sm_count()));
+  mk<<<blocks, kQueryThreads, p.bytes, s>>>(
+      t.view, d_types, static_cast<QueryRec<T> const*>(d_q), m, d_out, d_err,
+      p.stage_counts, p.stage_ranks);
+  EWT_LAUNCHED();
+}
+}  // namespace
+
+void launch_mixed_raw(ewt_tree& t, uint8_t const* d_types, void const* d_q,
+                      uint64_t m, uint64_t* d_out, uint32_t* d_err,
+                      cudaStream_t s) {
+  if (m == 0) return;
+  switch (t.elem_size) {
+    case 1: launch_mixed_raw_typed<uint8_t>(t, d_types, d_q, m, d_out, d_err, s); break;
+    case 2: launch_mixed_raw_typed<uint16_t>(t, d_types, d_q, m, d_out, d_err, s); break;
+    case 4: launch_mixed_raw_typed<uint32_t>(t, d_types, d_q, m, d_out, d_err, s); break;
+    default: launch_mixed_raw_typed<uint64_t>(t, d_types, d_q, m, d_out, d_err, s); break;
+  }
+}
+
 void launch_rs_rank(ewt_rs& r, int array, int value, uint64_t const* d_pos,
                     uint64_t m, uint64_t* d_out, cudaStream_t s) {
   if (m == 0) return;

@@ -149,6 +149,21 @@ int ewt_mixed_device(ewt_tree* tree, const uint8_t* d_types,
                      void* stream);
 int ewt_query_status(ewt_tree* tree, void* stream);
 
+/* ---- allocation-free mixed batch (no counterpart in the reference) ------
+ * Same inputs, results and statuses as ewt_mixed, for callers that must not
+ * allocate device memory while querying: code running while a stream is
+ * captured into a CUDA graph, serving loops whose arena or caching
+ * allocator owns all free HBM, and latency-critical paths where cudaFree's
+ * device-wide synchronisation would stall other streams.  The batch is
+ * staged in a fixed array compiled into libewt.so (about 6.3 MB on every
+ * GPU that loads it, held until exit); at most 262144 queries per call,
+ * larger batches return EWT_ERR_TOO_LARGE without touching the GPU.  The
+ * first call on a GPU looks up that array's device address; make it before
+ * any stream capture.  Calls share the array and are serialised; each
+ * returns after its GPU work is done.                                      */
+int ewt_mixed_noalloc(ewt_tree* tree, const uint8_t* types,
+                      const void* queries, uint64_t m, uint64_t* results);
+
 /* Copies the by-value device view (ecl::detail::TreeView) that the C++
  * header's WaveletTree<T> embeds; view_size must equal sizeof(TreeView).   */
 int ewt_get_device_view(const ewt_tree* tree, void* view_out,
