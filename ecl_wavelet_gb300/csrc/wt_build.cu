@@ -239,39 +239,57 @@ __device__ __forceinline__ bool level_bit(uint64_t c, uint32_t l, uint32_t L,
   return c >= node_of<false>(c, l, L, sigma).split;
 }
 
-// Level 0 bits: one thread per output word.  Check = validate symbols of a
-// minimal alphabet (c < sigma).
+// Level 0 bits: each thread writes fill_words<T>() output words (words
+// blockIdx.x * 256 * fill_words + threadIdx.x + 256 * j), with all their
+// symbol loads (128 bytes) issued before any is used.  Check = validate
+// symbols of a minimal alphabet (c < sigma).
+template <class T>
+__host__ __device__ constexpr uint32_t fill_words() {
+  return sizeof(T) == 1 ? 4u : (sizeof(T) == 2 ? 2u : 1u);
+}
+
 template <class T, bool Pow2, bool Check>
 __global__ void __launch_bounds__(256)
 fill0_kernel(T const* __restrict__ src, uint64_t size0, uint32_t L,
              uint64_t sigma, uint32_t* __restrict__ out,
              uint32_t* __restrict__ err) {
-  uint64_t const w = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
-  uint64_t const p0 = w * 32;
-  if (p0 >= size0) return;
-  uint32_t word = 0;
-  bool bad = false;
-  if (p0 + 32 <= size0) {
-    constexpr int kVec = 32 * sizeof(T) / 16;
-    uint4 buf[kVec];
-    uint4 const* s = reinterpret_cast<uint4 const*>(src + p0);
+  constexpr uint32_t kFillWords = fill_words<T>();
+  constexpr int kVec = 32 * sizeof(T) / 16;
+  uint64_t const base = uint64_t(blockIdx.x) * 256 * kFillWords + threadIdx.x;
+  uint4 buf[kFillWords][kVec];
 #pragma unroll
-    for (int q = 0; q < kVec; ++q) buf[q] = __ldg(s + q);
-    T const* e = reinterpret_cast<T const*>(buf);
+  for (uint32_t j = 0; j < kFillWords; ++j) {
+    uint64_t const p0 = (base + 256 * j) * 32;
+    if (p0 + 32 <= size0) {
+      uint4 const* s = reinterpret_cast<uint4 const*>(src + p0);
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      uint64_t const c = e[j];
-      if (Check) bad |= c >= sigma;
-      word |= uint32_t(level_bit<Pow2>(c, 0, L, sigma)) << j;
-    }
-  } else {
-    for (uint32_t j = 0; p0 + j < size0; ++j) {
-      uint64_t const c = src[p0 + j];
-      if (Check) bad |= c >= sigma;
-      word |= uint32_t(level_bit<Pow2>(c, 0, L, sigma)) << j;
+      for (int q = 0; q < kVec; ++q) buf[j][q] = __ldg(s + q);
     }
   }
-  out[w] = word;
+  bool bad = false;
+#pragma unroll
+  for (uint32_t j = 0; j < kFillWords; ++j) {
+    uint64_t const w = base + 256 * j;
+    uint64_t const p0 = w * 32;
+    if (p0 >= size0) break;
+    uint32_t word = 0;
+    if (p0 + 32 <= size0) {
+      T const* e = reinterpret_cast<T const*>(buf[j]);
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        uint64_t const c = e[i];
+        if (Check) bad |= c >= sigma;
+        word |= uint32_t(level_bit<Pow2>(c, 0, L, sigma)) << i;
+      }
+    } else {
+      for (uint32_t i = 0; p0 + i < size0; ++i) {
+        uint64_t const c = src[p0 + i];
+        if (Check) bad |= c >= sigma;
+        word |= uint32_t(level_bit<Pow2>(c, 0, L, sigma)) << i;
+      }
+    }
+    out[w] = word;
+  }
   if (Check && bad) atomicOr(err, 1u);
 }
 
@@ -303,9 +321,90 @@ level_nodes_kernel(TreeView t, LevelNode const* __restrict__ nodes,
 }  // namespace ewt
 
 #include "split.cuh"
+#include "passes.cuh"
 
 namespace ewt {
 namespace {
+
+// Levels 1 .. L-1 of a power-of-two alphabet by multi-level passes (see
+// passes.cuh); level 0 is already written.  Splits the L-1 levels into
+// ceil((L-1)/4) passes of near-equal size.
+template <class T>
+void run_passes(ewt_tree& t, T const* sym, uint64_t n, uint32_t* err,
+                cudaStream_t st) {
+  uint32_t const L = t.L;
+  uint32_t const levels = L - 1;
+  uint32_t const np = (levels + kPMaxK - 1) / kPMaxK;
+  uint32_t* const words = t.rs.words.as<uint32_t>();
+  uint64_t const w1 = t.rs.meta[1].word_off;
+  EWT_CUDA(cudaMemsetAsync(words + w1, 0, (t.rs.total_words - w1) * 4, st));
+  uint64_t const max_chunks = n / kPChunk + (uint64_t(1) << kPMaxStartLevel) + 2;
+  DevBuf chunk_first(((uint64_t(1) << kPMaxStartLevel) + 1) * 4);
+  DevBuf chunk_tot(max_chunks * kPMaxDigits * 4);
+  DevBuf chunk_pre(max_chunks * kPMaxDigits * 8);
+  DevBuf node_tot(((uint64_t(1) << kPMaxStartLevel) + 1) * kPMaxDigits * 8);
+  DevBuf order[2];
+  uint32_t const sms = static_cast<uint32_t>(sm_count());
+  T const* cur = sym;
+  uint32_t a = 0;
+  for (uint32_t i = 0; i < np; ++i) {
+    uint32_t const k = levels / np + (i < levels % np ? 1u : 0u);
+    uint32_t const b = a + k;
+    bool const write_order = b < L - 1;
+    EWT_REQUIRE(a <= kPMaxStartLevel && k >= 1 && k <= kPMaxK,
+                EWT_ERR_UNSUPPORTED, "pass plan out of range");
+    PassArgs pa{};
+    pa.n = n;
+    pa.L = L;
+    pa.a = a;
+    pa.k = k;
+    pa.nodes = 1u << a;
+    pa.words = words;
+    for (uint32_t r = 1; r <= k; ++r) {
+      pa.word_off[r] = t.rs.meta[a + r].word_off;
+      pa.nwords[r] = ceil_div(t.rs.meta[a + r].bits, 32);
+    }
+    pa.counts = t.counts_d.as<uint64_t>();
+    pa.chunk_first = chunk_first.as<uint32_t>();
+    pa.chunk_tot = chunk_tot.as<uint32_t>();
+    pa.chunk_pre = chunk_pre.as<uint64_t>();
+    pa.node_tot = node_tot.as<uint64_t>();
+    pa.err = err;
+    T* next = nullptr;
+    if (write_order) {
+      DevBuf& ob = order[i & 1];
+      if (!ob.get()) ob.alloc(n * sizeof(T) + 64);
+      next = ob.as<T>();
+    }
+    uint32_t const grid = static_cast<uint32_t>(
+        std::min<uint64_t>(max_chunks, uint64_t(sms) * 4));
+    {
+      PhaseTimer pt(EWT_PHASE_HIST, st);
+      chunk_table_kernel<<<1, 1024, 0, st>>>(pa);
+      EWT_LAUNCHED();
+      digit_count_kernel<T><<<static_cast<uint32_t>(std::min<uint64_t>(
+                                  max_chunks, uint64_t(sms) * 6)),
+                              kPThreads, 0, st>>>(cur, pa);
+      EWT_LAUNCHED();
+      pass_scan_kernel<<<pa.nodes << k, kScanThreads, 0, st>>>(pa);
+      EWT_LAUNCHED();
+      pass_counts_kernel<<<(pa.nodes + 255) / 256, 256, 0, st>>>(pa);
+      EWT_LAUNCHED();
+    }
+    {
+      PhaseTimer pt(EWT_PHASE_SPLIT, st);
+      auto kern = write_order ? pass_kernel<T, true> : pass_kernel<T, false>;
+      size_t const smem = pass_smem_bytes<T>();
+      EWT_CUDA(cudaFuncSetAttribute(
+          kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+          static_cast<int>(smem)));
+      kern<<<grid, kPThreads, smem, st>>>(cur, next, pa);
+      EWT_LAUNCHED();
+    }
+    cur = next;
+    a = b;
+  }
+}
 
 template <class T>
 void build_typed(ewt_tree& t, const void* data, uint64_t n,
@@ -523,7 +622,8 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   {
     PhaseTimer pt(EWT_PHASE_FILL, st);
     uint64_t const w0 = ceil_div(t.level_bits[0], 32);
-    uint32_t const blocks = static_cast<uint32_t>(ceil_div(w0, 256));
+    uint32_t const blocks =
+        static_cast<uint32_t>(ceil_div(w0, uint64_t(256) * fill_words<T>()));
     auto k = t.pow2 ? (t.is_min ? fill0_kernel<T, true, true>
                                 : fill0_kernel<T, true, false>)
                     : (t.is_min ? fill0_kernel<T, false, true>
@@ -533,17 +633,20 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
     EWT_LAUNCHED();
   }
   // ---- levels
-  DevBuf ping, pong;
-  if (L > 2) ping.alloc(n * sizeof(T));
-  if (L > 3) pong.alloc(n * sizeof(T));
-  T* bufs[2] = {ping.as<T>(), pong.as<T>()};
-  // tiles the fast split leaves to the general one, and their count
-  DevBuf slow_tiles((ceil_div(n, kSplitTile) + 1) * 4);
-  T const* src = sym;
-  for (uint32_t l = 0; l < L; ++l) {
-    build_rs_counts(t.rs, l, l + 1, st);
-    uint64_t const ncount = lv_off[l + 1] - lv_off[l];
-    if (ncount > 0) {
+  bool by_passes = false;
+  if constexpr (sizeof(T) <= 2) {
+    if (t.pow2 && L >= 2) {
+      run_passes<T>(t, sym, n, err_build, st);
+      by_passes = true;
+    }
+  }
+  if (by_passes) {
+    // All levels' bits came from the multi-level passes; now their counts
+    // and the node-start ranks (the count table is complete).
+    build_rs_counts(t.rs, 0, L, st);
+    for (uint32_t l = 0; l < L; ++l) {
+      uint64_t const ncount = lv_off[l + 1] - lv_off[l];
+      if (ncount == 0) continue;
       PhaseTimer pt(EWT_PHASE_NODE_RANKS, st);
       level_nodes_kernel<<<static_cast<uint32_t>(ceil_div(ncount, 128)), 128,
                            0, st>>>(v, lnodes_d.as<LevelNode>() + lv_off[l],
@@ -551,22 +654,42 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
                                     t.ranks_d.as<uint64_t>(), err_build);
       EWT_LAUNCHED();
     }
-    if (l + 1 < L) {
-      ArrayMeta const& mn = t.rs.meta[l + 1];
-      EWT_CUDA(cudaMemsetAsync(words + mn.word_off, 0,
-                               ceil_div(mn.bits, 32) * 4, st));
-      bool const write_order = l + 2 < L;
-      T* dst = write_order ? bufs[l & 1] : nullptr;
-      PhaseTimer pt(EWT_PHASE_SPLIT, st);
-      if (t.pow2)
-        launch_split<T, true>(write_order, src, dst, n, t.level_bits[l],
-                              mn.bits, l, v, words + mn.word_off,
-                              slow_tiles.as<uint32_t>(), err_build, st);
-      else
-        launch_split<T, false>(write_order, src, dst, n, t.level_bits[l],
-                               mn.bits, l, v, words + mn.word_off,
-                               slow_tiles.as<uint32_t>(), err_build, st);
-      src = dst;
+  } else {
+    DevBuf ping, pong;
+    if (L > 2) ping.alloc(n * sizeof(T));
+    if (L > 3) pong.alloc(n * sizeof(T));
+    T* bufs[2] = {ping.as<T>(), pong.as<T>()};
+    // tiles the fast split leaves to the general one, and their count
+    DevBuf slow_tiles((ceil_div(n, kSplitTile) + 1) * 4);
+    T const* src = sym;
+    for (uint32_t l = 0; l < L; ++l) {
+      build_rs_counts(t.rs, l, l + 1, st);
+      uint64_t const ncount = lv_off[l + 1] - lv_off[l];
+      if (ncount > 0) {
+        PhaseTimer pt(EWT_PHASE_NODE_RANKS, st);
+        level_nodes_kernel<<<static_cast<uint32_t>(ceil_div(ncount, 128)), 128,
+                             0, st>>>(v, lnodes_d.as<LevelNode>() + lv_off[l],
+                                      ncount, l, t.counts_d.as<uint64_t>(),
+                                      t.ranks_d.as<uint64_t>(), err_build);
+        EWT_LAUNCHED();
+      }
+      if (l + 1 < L) {
+        ArrayMeta const& mn = t.rs.meta[l + 1];
+        EWT_CUDA(cudaMemsetAsync(words + mn.word_off, 0,
+                                 ceil_div(mn.bits, 32) * 4, st));
+        bool const write_order = l + 2 < L;
+        T* dst = write_order ? bufs[l & 1] : nullptr;
+        PhaseTimer pt(EWT_PHASE_SPLIT, st);
+        if (t.pow2)
+          launch_split<T, true>(write_order, src, dst, n, t.level_bits[l],
+                                mn.bits, l, v, words + mn.word_off,
+                                slow_tiles.as<uint32_t>(), err_build, st);
+        else
+          launch_split<T, false>(write_order, src, dst, n, t.level_bits[l],
+                                 mn.bits, l, v, words + mn.word_off,
+                                 slow_tiles.as<uint32_t>(), err_build, st);
+        src = dst;
+      }
     }
   }
   build_rs_samples(t.rs, st);

@@ -1,0 +1,85 @@
+"""GPU parity of the multi-level build passes (power-of-two alphabets, 1- and
+2-byte symbols) against the CPU oracle, on the shapes that stress their
+bookkeeping: every level count L = 1..8 for uint8 and several for uint16,
+text lengths at tile (4096) and chunk (65536) boundaries, tiny texts, texts
+where most nodes are empty (one symbol, Zipf), and sorted / periodic texts
+whose tiles sit inside one class at every level.  Integer results: every
+exported structure byte-identical, every query equal to the plain scan.
+"""
+import numpy as np
+import pytest
+
+from tests.test_gpu_parity import assert_same_tree, check_queries
+
+pytestmark = pytest.mark.gpu
+
+
+def build_both(ewt, oracle, text, sigma):
+    alphabet = np.arange(sigma)
+    gt = ewt.WaveletTree(text, alphabet)
+    ot = oracle.OracleTree(text, alphabet)
+    assert_same_tree(gt, ot)
+    return gt, ot, alphabet.astype(np.uint64)
+
+
+@pytest.mark.parametrize("L", range(1, 9))
+def test_u8_every_level_count(ewt, oracle, L):
+    sigma = 1 << L
+    n = 2 * 65536 + 4097
+    rng = np.random.default_rng(L)
+    text = rng.integers(0, sigma, n, dtype=np.uint64).astype(np.uint8)
+    gt, ot, al = build_both(ewt, oracle, text, sigma)
+    check_queries(gt, ot, text, al, 5_000, seed=L)
+
+
+@pytest.mark.parametrize("n", [1, 2, 15, 16, 17, 4095, 4096, 4097, 65535,
+                               65536, 65537, 3 * 65536 + 4096])
+def test_u8_boundary_lengths(ewt, oracle, n):
+    rng = np.random.default_rng(n)
+    text = rng.integers(0, 256, n, dtype=np.uint64).astype(np.uint8)
+    gt, ot, al = build_both(ewt, oracle, text, 256)
+    check_queries(gt, ot, text, al, 2_000, seed=n)
+
+
+@pytest.mark.parametrize("L", [1, 5, 9, 13, 16])
+def test_u16_level_counts(ewt, oracle, L):
+    sigma = 1 << L
+    n = 200_003
+    rng = np.random.default_rng(100 + L)
+    text = rng.integers(0, sigma, n, dtype=np.uint64).astype(np.uint16)
+    gt, ot, al = build_both(ewt, oracle, text, sigma)
+    check_queries(gt, ot, text, al, 5_000, seed=L)
+
+
+@pytest.mark.parametrize("dtype,sigma", [(np.uint8, 256), (np.uint16, 65536)])
+def test_mostly_empty_nodes(ewt, oracle, dtype, sigma):
+    """Zipf(2) over the alphabet: deep nodes are empty or a few symbols."""
+    rng = np.random.default_rng(sigma)
+    w = 1.0 / np.arange(1, sigma + 1) ** 2.0
+    ids = rng.choice(sigma, 300_000, p=w / w.sum())
+    perm = rng.permutation(sigma)  # spread the frequent symbols over nodes
+    text = perm[ids].astype(dtype)
+    gt, ot, al = build_both(ewt, oracle, text, sigma)
+    check_queries(gt, ot, text, al, 5_000, seed=3)
+
+
+def test_single_symbol_text(ewt, oracle):
+    text = np.full(150_000, 200, np.uint8)
+    gt, ot, al = build_both(ewt, oracle, text, 256)
+    check_queries(gt, ot, text, al, 2_000, seed=4)
+
+
+@pytest.mark.parametrize("shape", ["sorted", "reversed", "periodic"])
+def test_structured_texts(ewt, oracle, shape):
+    n, sigma = 5 * 65536 + 123, 64
+    rng = np.random.default_rng(7)
+    base = rng.integers(0, sigma, n, dtype=np.uint64)
+    if shape == "sorted":
+        text = np.sort(base)
+    elif shape == "reversed":
+        text = np.sort(base)[::-1].copy()
+    else:
+        text = np.arange(n, dtype=np.uint64) % sigma
+    text = text.astype(np.uint8)
+    gt, ot, al = build_both(ewt, oracle, text, sigma)
+    check_queries(gt, ot, text, al, 2_000, seed=5)
