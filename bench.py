@@ -182,6 +182,31 @@ def run_reference(args, world, rank):
     print(json.dumps(line))
 
 
+def pass_plan(L):
+    """Levels emitted by each build pass: the L - 1 levels below level 0 in
+    ceil((L - 1) / 4) passes of near-equal size (as the library plans them)."""
+    levels = L - 1
+    if levels <= 0:
+        return []
+    np_ = (levels + 3) // 4
+    return [levels // np_ + (1 if i < levels % np_ else 0) for i in range(np_)]
+
+
+def pass_bytes_per_launch(n, L):
+    """Algorithmic HBM bytes of one pass launch over n uint8 symbols, averaged
+    over the passes: read the level order (n), write k levels of bits
+    (k * n / 8) and, unless it is the last pass, the next level order (n)."""
+    plan = pass_plan(L)
+    if not plan:
+        return 0.0
+    total, a = 0.0, 0
+    for k in plan:
+        b = a + k
+        total += n + k * n / 8.0 + (n if b < L - 1 else 0.0)
+        a = b
+    return total / len(plan)
+
+
 def make_mixed_queries(torch, tree, n, sigma, m, gen):
     """Device-resident mixed batch: types 40/40/20, RankSelectQuery records."""
     dev = "cuda"
@@ -258,12 +283,13 @@ def run_ours(args, world, rank, local):
     dom_ms, dom_launches = build_phases[dom]
     L = int(tree.getNumLevels())
     per_launch_bytes = {
-        # split: read the level order + write the next one (uint8 symbols)
-        "split": 2.0 * n,
+        # split: the multi-level passes (power-of-two alphabet, uint8)
+        "split": pass_bytes_per_launch(n, L),
         # fill: read the level order, write one bit per symbol
         "fill": n + n / 8.0,
         # rank/select counts: read one level's bits, write L2 + L1
         "rs_counts": n / 8.0 + 2.0 * n / 512 + 8.0 * n / 65536,
+        # digit counts of each pass: read the level order
         "hist": float(n),
         "samples": 2.0 * L * n / 512 + 16.0 * L * n / 4096,
         "node_ranks": 0.0,

@@ -113,6 +113,7 @@ SIGNATURES = {
     "ewt_rs_get_device_view": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "ewt_last_error": (C.c_char_p, []),
     "ewt_abi_version": (C.c_int, []),
+    "ewt_release_cached_memory": (C.c_int, [C.c_int]),
     "ewt_launch_count": (C.c_uint64, []),
     "ewt_set_timing": (None, [C.c_int]),
     "ewt_get_timing": (None, [C.c_void_p, C.c_int]),
@@ -175,6 +176,11 @@ def _ptr(a: np.ndarray) -> int:
 
 def launch_count() -> int:
     return int(lib().ewt_launch_count())
+
+
+def release_cached_memory(gpu_index: int = 0):
+    """Returns the library pool's unused device memory to the driver."""
+    _check(lib().ewt_release_cached_memory(gpu_index), "release_cached_memory")
 
 
 class WaveletTree:

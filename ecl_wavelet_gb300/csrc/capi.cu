@@ -15,6 +15,25 @@
 
 namespace ewt {
 
+cudaMemPool_t lib_pool() {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  int dev = 0;
+  EWT_CUDA(cudaGetDevice(&dev));
+  EWT_REQUIRE(dev >= 0 && dev < 64, EWT_ERR_INVALID_ARGUMENT, "device index out of range");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!pools[dev]) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    EWT_CUDA(cudaMemPoolCreate(&pools[dev], &props));
+    uint64_t keep = UINT64_MAX;
+    EWT_CUDA(cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep));
+  }
+  return pools[dev];
+}
+
 namespace {
 thread_local std::string g_last_error;
 std::atomic<uint64_t> g_launches{0};
@@ -106,6 +125,7 @@ int host_batch(ewt_tree* t, void const* in, size_t in_rec, uint8_t const* types,
                 "null query or result buffer");
     std::lock_guard<std::mutex> lk(t->query_mu);
     DeviceGuard g(t->device);
+    AllocStream as(t->stream);
     QueryScratch& sc = t->scratch;
     uint64_t const chunk = std::min(m, kChunk);
     ensure(sc.in, sc.in_cap, chunk * in_rec);
@@ -142,6 +162,7 @@ int rs_host_batch(ewt_rs* r, uint64_t const* in, uint64_t m, uint64_t* out,
                 "null query or result buffer");
     std::lock_guard<std::mutex> lk(r->query_mu);
     DeviceGuard g(r->device);
+    AllocStream as(r->stream);
     QueryScratch& sc = r->scratch;
     uint64_t const chunk = std::min(m, kChunk);
     ensure(sc.in, sc.in_cap, chunk * 8);
@@ -240,12 +261,17 @@ int ewt_build(const void* data, uint64_t n, int elem_size,
     auto t = std::make_unique<ewt_tree>();
     t->device = gpu_index;
     EWT_CUDA(cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking));
+    cudaStream_t const st = t->stream;
     try {
-      build_tree(*t, data, n, elem_size, alphabet, sigma, t->stream);
+      AllocStream as(st);
+      build_tree(*t, data, n, elem_size, alphabet, sigma, st);
     } catch (...) {
-      cudaStreamSynchronize(t->stream);
-      cudaStreamDestroy(t->stream);
-      t->stream = nullptr;
+      // buffers are returned to the pool in the stream's order, then the
+      // stream goes
+      cudaStreamSynchronize(st);
+      t.reset();
+      cudaStreamSynchronize(st);
+      cudaStreamDestroy(st);
       throw;
     }
     *out = t.release();
@@ -274,11 +300,13 @@ int ewt_free(ewt_tree* t) {
     if (!t) return;
     {
       DeviceGuard g(t->device);
-      if (t->stream) {
-        cudaStreamSynchronize(t->stream);
-        cudaStreamDestroy(t->stream);
+      cudaStream_t const st = t->stream;
+      if (st) cudaStreamSynchronize(st);
+      delete t;  // device buffers are freed in the stream's order
+      if (st) {
+        cudaStreamSynchronize(st);
+        cudaStreamDestroy(st);
       }
-      delete t;
     }
   });
 }
@@ -454,25 +482,37 @@ int ewt_rs_build(const uint32_t* words, const uint64_t* bits,
     auto r = std::make_unique<ewt_rs>();
     r->device = gpu_index;
     EWT_CUDA(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
-    r->err_d.alloc(16);
-    EWT_CUDA(cudaMemset(r->err_d.get(), 0, 16));
-    r->rs.layout(b);
-    if (is_device_pointer(words)) EWT_CUDA(cudaDeviceSynchronize());
-    uint64_t off = 0;
-    for (uint32_t a = 0; a < num_arrays; ++a) {
-      uint64_t const w = ceil_div(b[a], 32);
-      EWT_CUDA(cudaMemcpy(r->rs.words.as<uint32_t>() + r->rs.meta[a].word_off,
-                          words + off, w * 4, cudaMemcpyDefault));
-      off += w;
+    cudaStream_t const st = r->stream;
+    try {
+      AllocStream as(st);
+      r->err_d.alloc(16);
+      EWT_CUDA(cudaMemsetAsync(r->err_d.get(), 0, 16, st));
+      r->rs.layout(b);
+      if (is_device_pointer(words)) EWT_CUDA(cudaDeviceSynchronize());
+      uint64_t off = 0;
+      for (uint32_t a = 0; a < num_arrays; ++a) {
+        uint64_t const w = ceil_div(b[a], 32);
+        EWT_CUDA(cudaMemcpyAsync(r->rs.words.as<uint32_t>() + r->rs.meta[a].word_off,
+                                 words + off, w * 4, cudaMemcpyDefault, st));
+        off += w;
+      }
+      EWT_CUDA(cudaMemcpyAsync(r->rs.meta_d.get(), r->rs.meta.data(),
+                               num_arrays * sizeof(ArrayMeta),
+                               cudaMemcpyHostToDevice, st));
+      mask_tails_kernel<<<ceil_div(num_arrays, 128), 128, 0, st>>>(
+          r->rs.words.as<uint32_t>(), r->rs.meta_d.as<ArrayMeta>(), num_arrays);
+      EWT_LAUNCHED();
+      build_rs_counts(r->rs, 0, num_arrays, st);
+      build_rs_samples(r->rs, st);
+      build_rank_blocks(r->rs, st);
+      EWT_CUDA(cudaStreamSynchronize(st));
+    } catch (...) {
+      cudaStreamSynchronize(st);
+      r.reset();
+      cudaStreamSynchronize(st);
+      cudaStreamDestroy(st);
+      throw;
     }
-    EWT_CUDA(cudaMemcpy(r->rs.meta_d.get(), r->rs.meta.data(),
-                        num_arrays * sizeof(ArrayMeta), cudaMemcpyHostToDevice));
-    mask_tails_kernel<<<ceil_div(num_arrays, 128), 128, 0, r->stream>>>(
-        r->rs.words.as<uint32_t>(), r->rs.meta_d.as<ArrayMeta>(), num_arrays);
-    EWT_LAUNCHED();
-    build_rs_counts(r->rs, 0, num_arrays, r->stream);
-    build_rs_samples(r->rs, r->stream);
-    build_rank_blocks(r->rs, r->stream);
     *out = r.release();
   });
 }
@@ -481,11 +521,13 @@ int ewt_rs_free(ewt_rs* r) {
   return guarded([&] {
     if (!r) return;
     DeviceGuard g(r->device);
-    if (r->stream) {
-      cudaStreamSynchronize(r->stream);
-      cudaStreamDestroy(r->stream);
+    cudaStream_t const st = r->stream;
+    if (st) cudaStreamSynchronize(st);
+    delete r;  // device buffers are freed in the stream's order
+    if (st) {
+      cudaStreamSynchronize(st);
+      cudaStreamDestroy(st);
     }
-    delete r;
   });
 }
 
@@ -549,6 +591,14 @@ void ewt_get_timing(ewt_phase_times* out, int reset) {
 
 const char* ewt_last_error(void) { return g_last_error.c_str(); }
 int ewt_abi_version(void) { return EWT_ABI_VERSION; }
+
+int ewt_release_cached_memory(int gpu_index) {
+  return guarded([&] {
+    DeviceGuard g(gpu_index);
+    EWT_CUDA(cudaDeviceSynchronize());
+    EWT_CUDA(cudaMemPoolTrimTo(lib_pool(), 0));
+  });
+}
 uint64_t ewt_launch_count(void) { return g_launches.load(); }
 
 }  // extern "C"

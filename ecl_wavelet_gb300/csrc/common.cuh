@@ -55,18 +55,47 @@ inline int status_of(cudaError_t e) {
     if (!(cond)) throw ::ewt::Error((st), (msg));                           \
   } while (0)
 
-// Owning device allocation (cudaMalloc / cudaFree).
+// The stream that device allocations and frees of the running library
+// call are ordered on (set for the call's duration by AllocStream).
+inline cudaStream_t& alloc_stream() {
+  thread_local cudaStream_t s = nullptr;
+  return s;
+}
+class AllocStream {
+ public:
+  explicit AllocStream(cudaStream_t s) : prev_(alloc_stream()) { alloc_stream() = s; }
+  ~AllocStream() { alloc_stream() = prev_; }
+  AllocStream(AllocStream const&) = delete;
+  AllocStream& operator=(AllocStream const&) = delete;
+
+ private:
+  cudaStream_t prev_;
+};
+
+// Library memory pool of the current device: stream-ordered allocations
+// that keep freed blocks for reuse (release threshold: never), so repeated
+// builds do not pay cudaMalloc / cudaFree (whose frees synchronise the
+// device).  ewt_release_cached_memory() returns the cached blocks.
+cudaMemPool_t lib_pool();
+
+// Owning device allocation.  With an allocation stream set: from the
+// library pool, allocated and freed in that stream's order; otherwise
+// cudaMalloc / cudaFree.
 class DevBuf {
  public:
   DevBuf() = default;
   explicit DevBuf(size_t bytes) { alloc(bytes); }
   DevBuf(DevBuf const&) = delete;
   DevBuf& operator=(DevBuf const&) = delete;
-  DevBuf(DevBuf&& o) noexcept : p_(o.p_), n_(o.n_) { o.p_ = nullptr; o.n_ = 0; }
+  DevBuf(DevBuf&& o) noexcept
+      : p_(o.p_), n_(o.n_), s_(o.s_), pooled_(o.pooled_) {
+    o.p_ = nullptr;
+    o.n_ = 0;
+  }
   DevBuf& operator=(DevBuf&& o) noexcept {
     if (this != &o) {
       reset();
-      p_ = o.p_; n_ = o.n_;
+      p_ = o.p_; n_ = o.n_; s_ = o.s_; pooled_ = o.pooled_;
       o.p_ = nullptr; o.n_ = 0;
     }
     return *this;
@@ -75,11 +104,19 @@ class DevBuf {
   void alloc(size_t bytes) {
     reset();
     if (bytes == 0) bytes = 16;
-    EWT_CUDA(cudaMalloc(&p_, bytes));
+    s_ = alloc_stream();
+    pooled_ = s_ != nullptr;
+    if (pooled_)
+      EWT_CUDA(cudaMallocFromPoolAsync(&p_, bytes, lib_pool(), s_));
+    else
+      EWT_CUDA(cudaMalloc(&p_, bytes));
     n_ = bytes;
   }
   void reset() {
-    if (p_) cudaFree(p_);
+    if (p_) {
+      if (pooled_) cudaFreeAsync(p_, s_);
+      else cudaFree(p_);
+    }
     p_ = nullptr;
     n_ = 0;
   }
@@ -90,6 +127,8 @@ class DevBuf {
  private:
   void* p_ = nullptr;
   size_t n_ = 0;
+  cudaStream_t s_ = nullptr;
+  bool pooled_ = false;
 };
 
 // Owning pinned host allocation.

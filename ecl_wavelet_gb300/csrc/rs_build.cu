@@ -47,26 +47,29 @@ void RSStore::layout(std::vector<uint64_t> const& bits) {
   l1.alloc(total_l1 * 8);
   l2.alloc(total_l2 * 2);
   meta_d.alloc(meta.size() * sizeof(ArrayMeta));
-  EWT_CUDA(cudaMemcpy(meta_d.get(), meta.data(), meta.size() * sizeof(ArrayMeta),
-                      cudaMemcpyHostToDevice));
+  cudaStream_t const st = alloc_stream();
+  EWT_CUDA(cudaMemcpyAsync(meta_d.get(), meta.data(),
+                           meta.size() * sizeof(ArrayMeta),
+                           cudaMemcpyHostToDevice, st));
   std::vector<BlockJob> jobs(meta.size());
   for (size_t a = 0; a < meta.size(); ++a)
     jobs[a] = {meta[a].word_off, meta[a].bits, meta[a].l2_off, meta[a].l1_off,
                meta[a].num_l1, meta[a].num_last_l2};
   jobs_d.alloc(jobs.size() * sizeof(BlockJob));
-  EWT_CUDA(cudaMemcpy(jobs_d.get(), jobs.data(), jobs.size() * sizeof(BlockJob),
-                      cudaMemcpyHostToDevice));
+  EWT_CUDA(cudaMemcpyAsync(jobs_d.get(), jobs.data(),
+                           jobs.size() * sizeof(BlockJob),
+                           cudaMemcpyHostToDevice, st));
   // Zero the padding words behind every array (the arrays themselves are
   // written completely by their producer).
   for (auto const& m : meta) {
     uint64_t const w = ceil_div(m.bits, 32);
     uint64_t const padded = ceil_div(w, 32) * 32;
     if (padded > w)
-      EWT_CUDA(cudaMemset(words.as<uint32_t>() + m.word_off + w, 0,
-                          (padded - w) * 4));
+      EWT_CUDA(cudaMemsetAsync(words.as<uint32_t>() + m.word_off + w, 0,
+                               (padded - w) * 4, st));
   }
   if (total_words > 0 && total_words % 32)  // the even-rounding word
-    EWT_CUDA(cudaMemset(words.as<uint32_t>() + total_words - 1, 0, 4));
+    EWT_CUDA(cudaMemsetAsync(words.as<uint32_t>() + total_words - 1, 0, 4, st));
 }
 
 RSView RSStore::view() const {

@@ -214,6 +214,15 @@ int ewt_abi_version(void);
 /* Number of kernel launches this library issued since load (all threads). */
 uint64_t ewt_launch_count(void);
 
+/* Device memory of trees, rank/select structures, build scratch and query
+ * scratch comes from a library-owned, stream-ordered memory pool per GPU
+ * that keeps freed blocks for the next build instead of returning them to
+ * the driver (so repeated builds pay no cudaMalloc / cudaFree).  This call
+ * waits for the GPU and returns every unused cached block to the driver.
+ * No reference counterpart (the reference calls cudaMalloc / cudaFree
+ * directly, wavelet_tree.cuh:620-860). */
+int ewt_release_cached_memory(int gpu_index);
+
 #ifdef __cplusplus
 }
 #endif

@@ -83,3 +83,17 @@ def test_structured_texts(ewt, oracle, shape):
     text = text.astype(np.uint8)
     gt, ot, al = build_both(ewt, oracle, text, sigma)
     check_queries(gt, ot, text, al, 2_000, seed=5)
+
+
+def test_pool_reuse_and_release(ewt, oracle):
+    """Trees built after others were freed (their memory reused from the
+    library pool) and after the pool was trimmed are still exact."""
+    rng = np.random.default_rng(11)
+    text = rng.integers(0, 256, 300_000, dtype=np.uint64).astype(np.uint8)
+    ot = oracle.OracleTree(text, np.arange(256))
+    for i in range(3):
+        gt = ewt.WaveletTree(text, np.arange(256))
+        assert_same_tree(gt, ot)
+        gt.close()
+        if i == 1:
+            ewt.release_cached_memory(0)
