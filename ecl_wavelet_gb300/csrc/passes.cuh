@@ -665,10 +665,13 @@ pass_kernel(T const* __restrict__ src, T* __restrict__ dst, PassArgs p) {
             uint32_t ao = sbase + (T1s[c_first] + p0 - zt) * sizeof(T);
 #pragma unroll
             for (int i = 0; i < int(kItems); ++i) {
-              uint32_t const b = (bits >> i) & 1u;
-              st_shared<T>(b ? ao : az, e.get(i));
-              ao += b * sizeof(T);
-              az += (1u - b) * sizeof(T);
+              if ((bits >> i) & 1u) {
+                st_shared<T>(ao, e.get(i));
+                ao += sizeof(T);
+              } else {
+                st_shared<T>(az, e.get(i));
+                az += sizeof(T);
+              }
             }
           } else if (!to_fix) {
             // a tile's last, partial thread: per-symbol class lookup
