@@ -158,6 +158,18 @@ digit_count_kernel(T const* __restrict__ x, PassArgs p) {
       ++cnt_b[pass_digit<T>(x[i], dshift, dmask) * kPThreads + tid];
     uint4 const* v = reinterpret_cast<uint4 const*>(x + b0);
     uint64_t const nv = (b1 - b0) * sizeof(T) / 16;
+    // Counter d of this thread sits at byte d * 1024 + 4 * tid of each set;
+    // the digits of four bytes (two 16-bit symbols) come out of one SWAR
+    // shift-and-mask, each then costs one multiply-add for its address.
+    uint32_t const base_a = smem_u32(cnt_a) + 4 * tid;
+    uint32_t const base_b = smem_u32(cnt_b) + 4 * tid;
+    uint32_t const lanes_mask =
+        sizeof(T) == 1 ? 0x01010101u * dmask : 0x00010001u * dmask;
+    auto bump = [](uint32_t addr) {
+      uint32_t c;
+      asm volatile("ld.shared.u32 %0, [%1];" : "=r"(c) : "r"(addr) : "memory");
+      asm volatile("st.shared.u32 [%0], %1;" ::"r"(addr), "r"(c + 1) : "memory");
+    };
     // four 16-byte loads in flight per thread, then their symbols
     for (uint64_t i = tid; i < nv; i += 4 * kPThreads) {
       uint4 q[4];
@@ -172,12 +184,12 @@ digit_count_kernel(T const* __restrict__ x, PassArgs p) {
         uint32_t const w[4] = {q[u].x, q[u].y, q[u].z, q[u].w};
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
+          uint32_t const dw = (w[j] >> dshift) & lanes_mask;
 #pragma unroll
           for (int h = 0; h < int(4 / sizeof(T)); ++h) {
-            uint32_t const sym = sizeof(T) == 1 ? (w[j] >> (8 * h)) & 0xFFu
-                                                : (w[j] >> (16 * h)) & 0xFFFFu;
-            uint32_t const at = ((sym >> dshift) & dmask) * kPThreads + tid;
-            if (h & 1) ++cnt_b[at]; else ++cnt_a[at];
+            uint32_t const d =
+                (dw >> (8 * sizeof(T) * h)) & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu);
+            bump(((h & 1) ? base_b : base_a) + d * (kPThreads * 4));
           }
         }
       }

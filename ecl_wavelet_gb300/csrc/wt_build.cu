@@ -274,12 +274,33 @@ fill0_kernel(T const* __restrict__ src, uint64_t size0, uint32_t L,
     if (p0 >= size0) break;
     uint32_t word = 0;
     if (p0 + 32 <= size0) {
-      T const* e = reinterpret_cast<T const*>(buf[j]);
+      if constexpr (Pow2 && sizeof(T) <= 2) {
+        // SWAR: bit L-1 of four bytes (two 16-bit symbols) per operation;
+        // a symbol is >= sigma = 2^L iff it has a bit at or above L.
+        uint32_t const* w32 = reinterpret_cast<uint32_t const*>(buf[j]);
+        uint32_t const b = L - 1;
+        uint32_t const hi = sizeof(T) == 1
+                                ? 0x01010101u * ((0xFFu << L) & 0xFFu)
+                                : 0x00010001u * ((0xFFFFu << L) & 0xFFFFu);
 #pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        uint64_t const c = e[i];
-        if (Check) bad |= c >= sigma;
-        word |= uint32_t(level_bit<Pow2>(c, 0, L, sigma)) << i;
+        for (int i = 0; i < 8 * int(sizeof(T)); ++i) {
+          if (Check) bad |= (w32[i] & hi) != 0;
+          if constexpr (sizeof(T) == 1) {
+            uint32_t const t = (w32[i] >> b) & 0x01010101u;
+            word |= (((t * 0x00204081u) >> 21) & 0xFu) << (4 * i);
+          } else {
+            uint32_t const t = (w32[i] >> b) & 0x00010001u;
+            word |= ((t | (t >> 15)) & 3u) << (2 * i);
+          }
+        }
+      } else {
+        T const* e = reinterpret_cast<T const*>(buf[j]);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          uint64_t const c = e[i];
+          if (Check) bad |= c >= sigma;
+          word |= uint32_t(level_bit<Pow2>(c, 0, L, sigma)) << i;
+        }
       }
     } else {
       for (uint32_t i = 0; p0 + i < size0; ++i) {
