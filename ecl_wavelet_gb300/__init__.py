@@ -114,6 +114,15 @@ SIGNATURES = {
     "ewt_last_error": (C.c_char_p, []),
     "ewt_abi_version": (C.c_int, []),
     "ewt_release_cached_memory": (C.c_int, [C.c_int]),
+    "ewt_build_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_int,
+                                  C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                  C.c_void_p]),
+    "ewt_mixed_multi": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p,
+                                  C.c_void_p, C.c_void_p, C.c_uint64,
+                                  C.c_void_p]),
+    "ewt_mixed_multi_device": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_uint64,
+                                         C.c_void_p, C.c_void_p, C.c_void_p]),
     "ewt_launch_count": (C.c_uint64, []),
     "ewt_set_timing": (None, [C.c_int]),
     "ewt_get_timing": (None, [C.c_void_p, C.c_int]),
@@ -183,6 +192,54 @@ def release_cached_memory(gpu_index: int = 0):
     _check(lib().ewt_release_cached_memory(gpu_index), "release_cached_memory")
 
 
+_ELEM_DTYPE = {1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}
+
+
+def build_batch(texts, alphabets=None, gpu_index: int = 0):
+    """Builds many texts concurrently (ewt_build_batch); returns one
+    WaveletTree per text.  All texts share one symbol type; ``alphabets`` is
+    None (detect every alphabet) or one sorted alphabet per text."""
+    texts = [np.ascontiguousarray(t) for t in texts]
+    dt = texts[0].dtype
+    if any(t.dtype != dt for t in texts) or dt not in SYMBOL_DTYPES:
+        raise TypeError("texts must share one unsigned 8/16/32/64-bit type")
+    count = len(texts)
+    tp = (C.c_void_p * count)(*[_ptr(t) for t in texts])
+    lens = np.array([t.size for t in texts], dtype=np.uint64)
+    ap = sp = None
+    if alphabets is not None:
+        al = [np.ascontiguousarray(a, dtype=dt) for a in alphabets]
+        ap = (C.c_void_p * count)(*[_ptr(a) for a in al])
+        sig = np.array([a.size for a in al], dtype=np.uint64)
+        sp = _ptr(sig)
+    out = (C.c_void_p * count)()
+    st = np.zeros(count, dtype=np.int32)
+    rc = lib().ewt_build_batch(tp, _ptr(lens), count, dt.itemsize, ap, sp,
+                               gpu_index, out, _ptr(st))
+    trees = [WaveletTree(None, _handle=h) if h else None for h in out]
+    if rc != 0:
+        for t in trees:
+            if t is not None:
+                t.close()
+        _check(rc, "build_batch")
+    return trees
+
+
+def mixed_multi(trees, tree_of, types, queries) -> np.ndarray:
+    """Mixed queries over several trees in one launch (ewt_mixed_multi):
+    query i goes to trees[tree_of[i]]; records as WaveletTree.make_queries."""
+    count = len(trees)
+    hp = (C.c_void_p * count)(*[t._h.value for t in trees])
+    tree_of = np.ascontiguousarray(tree_of, dtype=np.uint32)
+    types = np.ascontiguousarray(types, dtype=np.uint8)
+    queries = np.ascontiguousarray(queries)
+    out = np.empty(types.size, dtype=np.uint64)
+    _check(lib().ewt_mixed_multi(hp, count, _ptr(tree_of), _ptr(types),
+                                 _ptr(queries), types.size, _ptr(out)),
+           "mixed_multi")
+    return out
+
+
 class WaveletTree:
     """ecl::WaveletTree<T> over a numpy text (uint8/16/32/64).
 
@@ -190,9 +247,17 @@ class WaveletTree:
     ``text`` may also be a torch CUDA tensor (built from device memory).
     """
 
-    def __init__(self, text, alphabet=None, gpu_index: int = 0):
+    def __init__(self, text, alphabet=None, gpu_index: int = 0, _handle=None):
         L = lib()
         self._h = C.c_void_p()
+        if _handle is not None:  # adopt a tree built by build_batch
+            self._h = C.c_void_p(_handle)
+            self._keep = None
+            self.info = Info()
+            _check(L.ewt_get_info(self._h, C.byref(self.info)), "get_info")
+            self.dtype = np.dtype(_ELEM_DTYPE[int(self.info.elem_size)])
+            self.qdtype = QUERY_DTYPE[self.dtype]
+            return
         if hasattr(text, "data_ptr"):  # torch tensor (host or device)
             dt = np.dtype(str(text.dtype).replace("torch.", ""))
             ptr, n = text.data_ptr(), text.numel()

@@ -7,6 +7,7 @@
 #include <atomic>
 #include <cstdint>
 #include <cstdio>
+#include <new>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -130,6 +131,26 @@ class DevBuf {
   cudaStream_t s_ = nullptr;
   bool pooled_ = false;
 };
+
+// Runs an entry point's body: library exceptions become an int status and
+// the calling thread's last-error message.
+template <class F>
+int run_guarded(F&& f) {
+  try {
+    f();
+    set_last_error("");
+    return EWT_OK;
+  } catch (Error const& e) {
+    set_last_error(e.what());
+    return e.status;
+  } catch (std::bad_alloc const&) {
+    set_last_error("host allocation failed");
+    return EWT_ERR_OUT_OF_MEMORY;
+  } catch (std::exception const& e) {
+    set_last_error(e.what());
+    return EWT_ERR_CUDA;
+  }
+}
 
 // Owning pinned host allocation.
 class PinnedBuf {

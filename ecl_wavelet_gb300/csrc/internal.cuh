@@ -111,6 +111,14 @@ void launch_mixed(ewt_tree& t, const uint8_t* d_types, const void* d_q,
 void launch_mixed_raw(ewt_tree& t, const uint8_t* d_types, const void* d_q,
                       uint64_t m, uint64_t* d_out, uint32_t* d_err,
                       cudaStream_t s);
+// Multi-tree mixed batch over an already grouped work list (multi.cu):
+// d_items holds num_items 16-byte items {uint32 tree, uint32 count, uint64
+// start} (count <= 2048) naming positions of d_q / d_types / d_out.
+void launch_multi_items(uint32_t elem_size, TreeView const* d_views,
+                        void const* d_items, uint32_t num_items,
+                        uint32_t max_levels, uint8_t const* d_types,
+                        void const* d_q, uint64_t* d_out, uint32_t* d_err,
+                        cudaStream_t s);
 void launch_rs_rank(ewt_rs& r, int array, int value, const uint64_t* d_pos,
                     uint64_t m, uint64_t* d_out, cudaStream_t s);
 void launch_rs_select(ewt_rs& r, int array, int value, const uint64_t* d_i,

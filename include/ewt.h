@@ -214,6 +214,34 @@ int ewt_abi_version(void);
 /* Number of kernel launches this library issued since load (all threads). */
 uint64_t ewt_launch_count(void);
 
+/* ---- many trees at once ------------------------------------------------
+ * Builds `count` texts (elem_size bytes per symbol) concurrently, each on its
+ * own stream: out[i] receives tree i (NULL when its build failed, with
+ * statuses[i], if given, holding its status).  alphabets / sigmas may be
+ * NULL (every alphabet detected).  Returns the first failing status.  The
+ * reference builds one tree per constructor call (wavelet_tree.cuh:576-867);
+ * no reference counterpart for the batch. */
+int ewt_build_batch(const void* const* texts, const uint64_t* lengths,
+                    uint32_t count, int elem_size,
+                    const void* const* alphabets, const uint64_t* sigmas,
+                    int gpu_index, ewt_tree** out, int* statuses);
+/* Mixed access/rank/select over several trees in one launch: query i is
+ * answered on trees[tree_of[i]] (types and records as ewt_mixed; results as
+ * ewt_mixed).  All trees share one symbol size and one GPU; fewer than 2^32
+ * queries, at most 65536 trees.  A tree id >= num_trees yields UINT64_MAX and
+ * EWT_ERR_QUERY.  Replaces one host call per tree (access/rank/select,
+ * wavelet_tree.cuh:956-1797); no single reference counterpart. */
+int ewt_mixed_multi(ewt_tree* const* trees, uint32_t num_trees,
+                    const uint32_t* tree_of, const uint8_t* types,
+                    const void* queries, uint64_t m, uint64_t* results);
+/* Same over device buffers on `stream` (a cudaStream_t); asynchronous.
+ * *d_err (device) is OR-ed with 1 for invalid queries and 2 for unknown
+ * tree ids; the caller clears and reads it. */
+int ewt_mixed_multi_device(ewt_tree* const* trees, uint32_t num_trees,
+                           const uint32_t* d_tree_of, const uint8_t* d_types,
+                           const void* d_queries, uint64_t m,
+                           uint64_t* d_results, uint32_t* d_err, void* stream);
+
 /* Device memory of trees, rank/select structures, build scratch and query
  * scratch comes from a library-owned, stream-ordered memory pool per GPU
  * that keeps freed blocks for the next build instead of returning them to
