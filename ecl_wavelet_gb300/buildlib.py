@@ -18,6 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 OBJ_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libewt.so")
+SCHED_LIB = os.path.join(PKG, "libewt_sched.so")  # CUDA-free scheduler core
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
@@ -32,11 +33,13 @@ def nvcc() -> str:
 
 
 def sources():
-    return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    return sorted(glob.glob(os.path.join(CSRC, "*.cu"))
+                  + glob.glob(os.path.join(CSRC, "*.cpp")))
 
 
 def headers():
     return (glob.glob(os.path.join(CSRC, "*.cuh"))
+            + glob.glob(os.path.join(CSRC, "*.h"))
             + glob.glob(os.path.join(INCLUDE, "**", "*.h*"), recursive=True))
 
 
@@ -72,9 +75,26 @@ def build(verbose: bool = False, extra_flags=()) -> str:
             raise RuntimeError("nvcc link failed:\n%s\n%s" % (" ".join(cmd),
                                                             r.stderr[-4000:]))
         os.replace(tmp, LIB)
+    build_sched()
     if verbose:
         print("built", LIB)
     return LIB
+
+
+def build_sched() -> str:
+    """Builds libewt_sched.so (the serving scheduler core, no CUDA) with the
+    host C++ compiler, so its tests run on hosts without a GPU or nvcc."""
+    src = os.path.join(CSRC, "sched_capi.cpp")
+    deps = [src, os.path.join(CSRC, "serve_sched.h"), os.path.join(INCLUDE, "ewt_sched.h")]
+    if _stale(SCHED_LIB, deps):
+        tmp = SCHED_LIB + ".tmp%d" % os.getpid()
+        cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-shared",
+               "-I", INCLUDE, "-I", CSRC, src, "-o", tmp]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("g++ failed:\n%s\n%s" % (" ".join(cmd), r.stderr[-4000:]))
+        os.replace(tmp, SCHED_LIB)
+    return SCHED_LIB
 
 
 if __name__ == "__main__":

@@ -171,6 +171,7 @@ class PinnedBuf {
     n_ = 0;
   }
   template <class T> T* as() const { return static_cast<T*>(p_); }
+  void* get() const { return p_; }
   size_t bytes() const { return n_; }
 
  private:

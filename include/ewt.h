@@ -55,6 +55,7 @@ extern "C" {
 #define EWT_ERR_UNSUPPORTED (-6)
 #define EWT_ERR_TIMEOUT (-7) /* a bounded device-side wait gave up        */
 #define EWT_ERR_TOO_LARGE (-8) /* size beyond a stated fixed maximum      */
+#define EWT_ERR_CANCELLED (-9) /* the request was cancelled before it ran */
 
 /* ---- query types of the mixed batch ----------------------------------- */
 #define EWT_Q_ACCESS 0
@@ -241,6 +242,85 @@ int ewt_mixed_multi_device(ewt_tree* const* trees, uint32_t num_trees,
                            const uint32_t* d_tree_of, const uint8_t* d_types,
                            const void* d_queries, uint64_t m,
                            uint64_t* d_results, uint32_t* d_err, void* stream);
+
+/* ---- serving engine ---------------------------------------------------
+ * Resident trees, query requests served by continuous batching, builds
+ * admitted by device-memory footprint, p50/p99 latency.  A dispatcher thread
+ * packs every pending request that fits into the next free batch slot
+ * (`inflight` slots, each its own stream and pinned buffers) and launches
+ * one multi-tree kernel per batch; a completer thread hands results back;
+ * a builder thread runs admitted builds.  Requests arriving while batches
+ * run join the next batch.  No reference counterpart (the reference serves
+ * one synchronous host call at a time, wavelet_tree.cuh:956-1797). */
+#include "ewt_sched.h"
+typedef struct ewt_server ewt_server;
+typedef struct ewt_server_config {
+  uint64_t batch_queries;  /* queries per batch; also the largest request */
+  uint32_t batch_requests; /* requests per batch                         */
+  uint32_t inflight;       /* batches on the GPU at once, 1 .. 8           */
+  uint64_t memory_budget;  /* device bytes for resident trees and builds   */
+  uint32_t elem_size;      /* symbol size of every tree served             */
+} ewt_server_config;
+int ewt_server_create(int gpu_index, const ewt_server_config* cfg,
+                      ewt_server** out);
+/* Serves what was submitted, stops the threads, frees the trees the server
+ * built (trees added by the caller stay the caller's). */
+int ewt_server_destroy(ewt_server* s);
+/* Registers a built tree (the caller keeps ownership and must keep it alive
+ * until it is removed or the server destroyed); its device bytes count
+ * against the budget. */
+int ewt_server_add_tree(ewt_server* s, ewt_tree* tree, uint32_t* tree_id);
+/* Waits until no queued or running batch can reference the tree, then
+ * unregisters it (and frees it when the server built it). */
+int ewt_server_remove_tree(ewt_server* s, uint32_t tree_id);
+/* Queues m (1 .. batch_queries) mixed queries (types and records as
+ * ewt_mixed) against a registered tree.  Host buffers; they must stay valid,
+ * and results untouched, until the request completes. */
+int ewt_server_submit(ewt_server* s, uint32_t tree_id, const uint8_t* types,
+                      const void* queries, uint64_t m, uint64_t* results,
+                      uint64_t* request_id);
+/* Queues the build of a text (host or device pointer; alphabet as
+ * ewt_build); it starts when its estimated footprint fits the budget. */
+int ewt_server_submit_build(ewt_server* s, const void* text, uint64_t n,
+                            const void* alphabet, uint64_t sigma,
+                            uint64_t* request_id);
+/* Blocks until the request completed or was cancelled; *status receives its
+ * status (EWT_ERR_QUERY when it held invalid queries, EWT_ERR_CANCELLED),
+ * *latency_ms submit-to-completion time, *tree_id the id of a built tree.
+ * Any out pointer may be NULL.  A request can be waited for once. */
+int ewt_server_wait(ewt_server* s, uint64_t request_id, int* status,
+                    double* latency_ms, uint32_t* tree_id);
+/* Cancels a request that has not started (EWT_ERR_INVALID_ARGUMENT if it
+ * already runs or is unknown). */
+int ewt_server_cancel(ewt_server* s, uint64_t request_id);
+/* Counters and latency percentiles of the completed requests; reset != 0
+ * clears the latency record afterwards. */
+int ewt_server_stats(ewt_server* s, ewt_sched_stats* out, int reset);
+
+/* Native load generator: Poisson arrivals of requests of log-uniform size,
+ * each against a uniformly chosen tree of [first_tree, first_tree +
+ * num_trees), queries drawn from valid ranges with the given access / rank
+ * fractions (the rest select).  plain != 0 serves the same arrivals through
+ * the plain per-request path instead: one synchronous ewt_mixed call per
+ * request, in arrival order.  build_n > 0 adds the build of a sigma-4 uint8
+ * text of build_n symbols every build_interval_s. */
+typedef struct ewt_load_config {
+  double rate, duration_s;
+  uint32_t max_request, first_tree, num_trees;
+  double frac_access, frac_rank;
+  uint64_t seed;
+  int plain;
+  uint64_t build_n;
+  double build_interval_s;
+} ewt_load_config;
+typedef struct ewt_load_result {
+  uint64_t requests, queries;
+  double wall_s, qps, p50_ms, p99_ms, mean_ms, max_ms;
+  uint64_t batches, builds;
+  double build_p50_ms;
+} ewt_load_result;
+int ewt_server_run_load(ewt_server* s, const ewt_load_config* cfg,
+                        ewt_load_result* res);
 
 /* Device memory of trees, rank/select structures, build scratch and query
  * scratch comes from a library-owned, stream-ordered memory pool per GPU
