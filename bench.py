@@ -48,6 +48,10 @@ def parse():
     p.add_argument("--queries", type=int, default=1 << 26)
     p.add_argument("--no-sweep", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-multi", action="store_true",
+                   help="skip the many-text build and multi-tree queries")
+    p.add_argument("--no-serve", action="store_true",
+                   help="skip the serving-loop rate sweep")
     p.add_argument("--cpu-sample", type=int, default=1 << 25)
     p.add_argument("--only", default="all", choices=["all", "build", "queries"],
                    help="build: stop after the timed builds; queries: also "
@@ -205,6 +209,148 @@ def pass_bytes_per_launch(n, L):
         total += n + k * n / 8.0 + (n if b < L - 1 else 0.0)
         a = b
     return total / len(plan)
+
+
+def bench_multi_text(torch, E, dev, gen, seed=7):
+    """256 uint8 texts, lengths log-uniform in [2^16, 2^26], sigma per text
+    from {4, 16, 64, 256}, device-resident: batched build vs one build per
+    text, then 2^24 mixed queries (text chosen in proportion to its length)
+    in one multi-tree launch vs one launch per text."""
+    import ctypes
+    rng = np.random.default_rng(seed)
+    T = 256
+    lens = np.floor(np.exp(rng.uniform(np.log(2 ** 16), np.log(2 ** 26), T))).astype(np.int64)
+    sig = rng.choice([4, 16, 64, 256], T)
+    texts = [torch.randint(0, int(s_), (int(n_),), dtype=torch.uint8, device=dev,
+                           generator=gen) for n_, s_ in zip(lens, sig)]
+    alph = [np.arange(int(s_)) for s_ in sig]
+    total = int(lens.sum())
+    torch.cuda.synchronize()
+    for t in E.build_batch(texts[:16], alph[:16]):
+        t.close()
+    a = time.perf_counter()
+    plain = [E.WaveletTree(t, al) for t, al in zip(texts, alph)]
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - a
+    for t in plain:
+        t.close()
+    a = time.perf_counter()
+    trees = E.build_batch(texts, alph)
+    torch.cuda.synchronize()
+    batch_s = time.perf_counter() - a
+    # 2^24 mixed queries, 40/40/20, text in proportion to its length
+    m = 1 << 24
+    tree_of = rng.choice(T, m, p=lens / lens.sum()).astype(np.uint32)
+    ty = rng.choice(3, m, p=[0.4, 0.4, 0.2]).astype(np.uint8)
+    n_t = lens[tree_of]
+    s_t = sig[tree_of]
+    u = rng.random(m)
+    c = (rng.random(m) * s_t).astype(np.int64)
+    occ = np.zeros((T, 256), np.int64)
+    for i, t in enumerate(trees):
+        cnt = t.export("COUNTS").astype(np.int64)
+        occ[i, :sig[i]] = np.diff(np.append(cnt, lens[i]))
+    k = 1 + (u * np.maximum(occ[tree_of, c], 1)).astype(np.int64)
+    index = np.where(ty == 0, (u * n_t).astype(np.int64),
+                     np.where(ty == 1, (u * (n_t + 1)).astype(np.int64), k))
+    rec = np.zeros(m, dtype=trees[0].qdtype)
+    rec["index"] = index
+    rec["symbol"] = c
+    d_tree = torch.from_numpy(tree_of.view(np.int32)).to(dev)
+    d_ty = torch.from_numpy(ty).to(dev)
+    d_q = torch.from_numpy(rec.view(np.uint8)).to(dev)
+    d_out = torch.empty(m, dtype=torch.int64, device=dev)
+    d_err = torch.zeros(1, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream()
+    hp = (ctypes.c_void_p * T)(*[t.handle for t in trees])
+    L = E.lib()
+
+    def multi():
+        st = L.ewt_mixed_multi_device(hp, T, d_tree.data_ptr(), d_ty.data_ptr(),
+                                      d_q.data_ptr(), m, d_out.data_ptr(),
+                                      d_err.data_ptr(), stream.cuda_stream)
+        assert st == 0
+
+    # the same queries grouped per text for the plain per-text launches
+    order = np.argsort(tree_of, kind="stable")
+    bounds = np.searchsorted(tree_of[order], np.arange(T + 1))
+    g_ty = torch.from_numpy(ty[order]).to(dev)
+    g_q = torch.from_numpy(rec[order].view(np.uint8)).to(dev)
+    g_out = torch.empty(m, dtype=torch.int64, device=dev)
+
+    def per_text():
+        for i, t in enumerate(trees):
+            b0, b1 = int(bounds[i]), int(bounds[i + 1])
+            if b1 > b0:
+                t.mixed_device(g_ty.data_ptr() + b0, g_q.data_ptr() + 16 * b0,
+                               b1 - b0, g_out.data_ptr() + 8 * b0,
+                               stream.cuda_stream)
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    multi_ms = timed(multi)
+    assert int(d_err.item()) == 0
+    plain_ms = timed(per_text)
+    # both forms answer identically
+    assert torch.equal(d_out[torch.from_numpy(order).to(dev)], g_out)
+    for t in trees:
+        t.close()
+    return {"texts": T, "symbols": total,
+            "batched_build_ms": batch_s * 1e3,
+            "per_text_build_ms": plain_s * 1e3,
+            "batched_build_GB_s": total / batch_s / 1e9,
+            "per_text_build_GB_s": total / plain_s / 1e9,
+            "queries": m,
+            "multi_tree_Mq_s": m / multi_ms / 1e3,
+            "per_text_launches_Mq_s": m / plain_ms / 1e3,
+            "multi_over_per_text": plain_ms / multi_ms}
+
+
+def bench_serving(torch, E, dev, gen, big_text):
+    """A 6*2^30-symbol sigma-256 index plus 64 sigma-4 texts of 2^26 symbols
+    resident; Poisson arrivals of requests of log-uniform 1..2^16 mixed
+    queries (40/40/20) at swept rates, served by the engine (continuous
+    batching) and, at the lower rates, by the plain per-request path; build
+    requests of 2^24-symbol texts arrive every 0.25 s at one rate."""
+    from ecl_wavelet_gb300.serving import Server
+    big = E.WaveletTree(big_text, np.arange(256))
+    small_texts = [torch.randint(0, 4, (1 << 26,), dtype=torch.uint8, device=dev,
+                                 generator=gen) for _ in range(64)]
+    smalls = E.build_batch(small_texts, [np.arange(4)] * 64)
+    srv = Server(batch_queries=1 << 20, batch_requests=1 << 12, inflight=3,
+                 memory_budget=200 << 30, elem_size=1)
+    srv.add_tree(big)
+    for t in smalls:
+        srv.add_tree(t)
+    out = []
+    for rate in (1000, 4000, 16000, 64000, 256000):
+        e = {"rate_rps": rate,
+             "engine": srv.run_load(rate=rate, duration_s=1.0, num_trees=65,
+                                    seed=rate,
+                                    build_n=(1 << 24) if rate == 16000 else 0,
+                                    build_interval_s=0.25)}
+        if rate <= 16000:
+            e["plain"] = srv.run_load(rate=rate, duration_s=0.5, num_trees=65,
+                                      seed=rate, plain=True)
+        out.append(e)
+    srv.close()
+    big.close()
+    for t in smalls:
+        t.close()
+    return {"resident": "1 x 6*2^30 sigma-256 + 64 x 2^26 sigma-4 (uint8)",
+            "request_sizes": "log-uniform 1..65536, 40/40/20 access/rank/select",
+            "server": {"batch_queries": 1 << 20, "inflight": 3},
+            "sweep": out}
 
 
 def make_mixed_queries(torch, tree, n, sigma, m, gen):
@@ -434,6 +580,13 @@ def run_ours(args, world, rank, local):
             sweep[str(s)] = n / (time.perf_counter() - a) / 1e9
             del t2
 
+    # ---- many texts and serving (one GPU's share) --------------------------
+    multi = serve = None
+    if not args.no_multi:
+        multi = bench_multi_text(torch, E, dev, gen)
+    if not args.no_serve:
+        serve = bench_serving(torch, E, dev, gen, text)
+
     # ---- CPU baseline (rank 0, N = 1 only) ---------------------------------
     if rank == 0 and world == 1 and not args.no_cpu:
         from oracle import oracle as O
@@ -472,6 +625,7 @@ def run_ours(args, world, rank, local):
             "gpu_launches": launches,
             "roofline": roofline, "build": build, "queries": queries,
             "sigma_sweep_GB_s": sweep, "e2e": e2e, "cpu_baseline": cpu,
+            "many_texts": multi, "serving": serve,
             "clocks": clk,
         }
         print(json.dumps(line))

@@ -199,13 +199,22 @@ def build_batch(texts, alphabets=None, gpu_index: int = 0):
     """Builds many texts concurrently (ewt_build_batch); returns one
     WaveletTree per text.  All texts share one symbol type; ``alphabets`` is
     None (detect every alphabet) or one sorted alphabet per text."""
-    texts = [np.ascontiguousarray(t) for t in texts]
-    dt = texts[0].dtype
-    if any(t.dtype != dt for t in texts) or dt not in SYMBOL_DTYPES:
-        raise TypeError("texts must share one unsigned 8/16/32/64-bit type")
+    if all(hasattr(t, "data_ptr") for t in texts):  # torch tensors
+        dt = np.dtype(str(texts[0].dtype).replace("torch.", ""))
+        ptrs = [t.data_ptr() for t in texts]
+        sizes = [t.numel() for t in texts]
+    else:
+        texts = [np.ascontiguousarray(t) for t in texts]
+        dt = texts[0].dtype
+        if any(t.dtype != dt for t in texts):
+            raise TypeError("texts must share one symbol type")
+        ptrs = [_ptr(t) for t in texts]
+        sizes = [t.size for t in texts]
+    if dt not in SYMBOL_DTYPES:
+        raise TypeError("texts must hold unsigned 8/16/32/64-bit symbols")
     count = len(texts)
-    tp = (C.c_void_p * count)(*[_ptr(t) for t in texts])
-    lens = np.array([t.size for t in texts], dtype=np.uint64)
+    tp = (C.c_void_p * count)(*ptrs)
+    lens = np.array(sizes, dtype=np.uint64)
     ap = sp = None
     if alphabets is not None:
         al = [np.ascontiguousarray(a, dtype=dt) for a in alphabets]
