@@ -332,6 +332,8 @@ def bench_serving(torch, E, dev, gen, big_text):
     srv.add_tree(big)
     for t in smalls:
         srv.add_tree(t)
+    srv.run_load(rate=2000, duration_s=0.3, num_trees=65, seed=99)  # warm-up
+    srv.run_load(rate=2000, duration_s=0.3, num_trees=65, seed=99, plain=True)
     out = []
     for rate in (1000, 4000, 16000, 64000, 256000):
         e = {"rate_rps": rate,

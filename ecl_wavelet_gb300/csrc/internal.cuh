@@ -119,6 +119,15 @@ void launch_multi_items(uint32_t elem_size, TreeView const* d_views,
                         uint32_t max_levels, uint8_t const* d_types,
                         void const* d_q, uint64_t* d_out, uint32_t* d_err,
                         cudaStream_t s);
+// Zero-copy serving launch (multi.cu): `reqs` holds 32-byte descriptors
+// {const uint8_t* types; const void* queries; uint64_t* results; uint32
+// tree; uint32 pad} of buffers the GPU reads and writes in place, `items`
+// 16-byte {uint32 req, uint32 count (<= 2048), uint64 start}; req_err[r] is
+// set to 1 when request r held an invalid query.
+void launch_serve_items(uint32_t elem_size, TreeView const* d_views,
+                        void const* reqs, void const* items, uint32_t num_items,
+                        uint32_t max_levels, uint32_t* req_err, cudaStream_t s);
+void prepare_serve_kernels(uint32_t elem_size);
 void launch_rs_rank(ewt_rs& r, int array, int value, const uint64_t* d_pos,
                     uint64_t m, uint64_t* d_out, cudaStream_t s);
 void launch_rs_select(ewt_rs& r, int array, int value, const uint64_t* d_i,

@@ -248,6 +248,132 @@ multi_kernel(TreeView const* __restrict__ views,
   if (bad) atomicOr(err, 1u);
 }
 
+// Zero-copy form for the serving engine: work items name a request whose
+// descriptor points at the caller's buffers (host memory the GPU reads and
+// writes in place when it can access pageable memory); invalid queries set
+// the request's error flag.
+struct ServeReq {
+  uint8_t const* types;
+  void const* queries;
+  uint64_t* results;
+  uint32_t tree, pad;
+};
+struct ServeItemD {
+  uint32_t req, count;
+  uint64_t start;
+};
+
+template <class T>
+__global__ void __launch_bounds__(kMultiThreads)
+serve_kernel(TreeView const* __restrict__ views, ServeReq const* __restrict__ reqs,
+             ServeItemD const* __restrict__ items, uint32_t n_items,
+             uint32_t* __restrict__ req_err) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ __align__(8) TreeView tv;
+  __shared__ ServeItemD it;
+  __shared__ ServeReq rq;
+  __shared__ uint16_t lists[3][kMultiChunk];
+  __shared__ uint32_t list_len[3];
+  uint32_t const tid = threadIdx.x, lane = tid & 31;
+  uint32_t const lt = (1u << lane) - 1u;
+  for (uint32_t w = blockIdx.x; w < n_items; w += gridDim.x) {
+    if (tid == 0) {
+      it = items[w];
+      rq = reqs[it.req];
+    }
+    if (tid < 3) list_len[tid] = 0;
+    __syncthreads();
+    ServeItemD const item = it;
+    uint8_t const* types = rq.types + item.start;
+    MultiRec<T> const* in = static_cast<MultiRec<T> const*>(rq.queries) + item.start;
+    uint64_t* out = rq.results + item.start;
+    {
+      uint64_t const* src = reinterpret_cast<uint64_t const*>(views + rq.tree);
+      uint64_t* dst = reinterpret_cast<uint64_t*>(&tv);
+      for (uint32_t i = tid; i < sizeof(TreeView) / 8; i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    uint32_t const L = tv.levels;
+    ArrayMeta* meta = reinterpret_cast<ArrayMeta*>(smem);
+    uint64_t* node_base = reinterpret_cast<uint64_t*>(meta + L);
+    {
+      uint64_t const* gm = reinterpret_cast<uint64_t const*>(tv.rs.meta);
+      uint64_t* sm = reinterpret_cast<uint64_t*>(meta);
+      for (uint32_t i = tid; i < L * (sizeof(ArrayMeta) / 8); i += blockDim.x) sm[i] = gm[i];
+      for (uint32_t i = tid; i <= L; i += blockDim.x) node_base[i] = tv.node_base[i];
+    }
+    uint32_t bad = 0;
+    for (uint32_t j = tid; j < kMultiChunk; j += blockDim.x) {
+      uint32_t const ty = j < item.count ? types[j] : 3u;
+#pragma unroll
+      for (uint32_t k = 0; k < 3; ++k) {
+        uint32_t const mask = __ballot_sync(0xffffffffu, ty == k);
+        if (mask == 0) continue;
+        uint32_t pos = 0;
+        if (lane == __ffs(mask) - 1) pos = atomicAdd(&list_len[k], __popc(mask));
+        pos = __shfl_sync(0xffffffffu, pos, __ffs(mask) - 1);
+        if (ty == k) lists[k][pos + __popc(mask & lt)] = static_cast<uint16_t>(j);
+      }
+      if (ty > 2 && j < item.count) {
+        out[j] = UINT64_MAX;
+        bad = 1;
+      }
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < list_len[0]; i += blockDim.x) {
+      uint32_t const j = lists[0][i];
+      uint64_t const idx = in[j].index;
+      out[j] = idx < tv.n ? static_cast<uint64_t>(from_minimal<T>(
+                                tv, wt_access(tv, meta, tv.counts, tv.node_ranks,
+                                              node_base, idx)))
+                          : 0;
+    }
+    for (uint32_t i = tid; i < list_len[1]; i += blockDim.x) {
+      uint32_t const j = lists[1][i];
+      MultiRec<T> const r = in[j];
+      uint64_t const sym = to_minimal<T>(tv, r.symbol);
+      if (sym >= tv.sigma || r.index > tv.n) {
+        out[j] = UINT64_MAX;
+        bad = 1;
+      } else {
+        out[j] = wt_rank(tv, meta, tv.counts, tv.node_ranks, node_base, sym, r.index);
+      }
+    }
+    for (uint32_t i = tid; i < list_len[2]; i += blockDim.x) {
+      uint32_t const j = lists[2][i];
+      MultiRec<T> const r = in[j];
+      uint64_t const sym = to_minimal<T>(tv, r.symbol);
+      if (sym >= tv.sigma || r.index == 0) {
+        out[j] = UINT64_MAX;
+        bad = 1;
+      } else {
+        out[j] = wt_select(tv, meta, tv.counts, tv.node_ranks, node_base, sym, r.index);
+      }
+    }
+    if (bad) req_err[item.req] = 1u;  // the same value from every writer
+    __syncthreads();  // tv, rq, meta and lists are reused by the next item
+  }
+}
+
+template <class T>
+void launch_serve_typed(TreeView const* views, ServeReq const* reqs,
+                        ServeItemD const* items, uint32_t n_items,
+                        uint32_t max_levels, uint32_t* req_err, cudaStream_t s) {
+  size_t const smem = max_levels * sizeof(ArrayMeta) + (max_levels + 1) * 8;
+  thread_local int cached[65] = {};
+  int& per_sm = cached[std::min<uint32_t>(max_levels, 64)];
+  if (per_sm == 0) {
+    EWT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, serve_kernel<T>, kMultiThreads, smem));
+    per_sm = std::max(per_sm, 1);
+  }
+  uint32_t const blocks = static_cast<uint32_t>(std::max<uint64_t>(
+      1, std::min<uint64_t>(n_items, uint64_t(per_sm) * sm_count())));
+  serve_kernel<T><<<blocks, kMultiThreads, smem, s>>>(views, reqs, items, n_items,
+                                                      req_err);
+  EWT_LAUNCHED();
+}
+
 template <class T>
 void launch_multi_typed(TreeView const* d_views, MultiItem const* d_items,
                         uint32_t const* d_num_items, uint32_t h_num_items,
@@ -256,10 +382,14 @@ void launch_multi_typed(TreeView const* d_views, MultiItem const* d_items,
                         void const* d_q, uint64_t* d_out, uint32_t* d_err,
                         cudaStream_t s) {
   size_t const smem = max_levels * sizeof(ArrayMeta) + (max_levels + 1) * 8;
-  int per_sm = 0;
-  EWT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &per_sm, multi_kernel<T>, kMultiThreads, smem));
-  per_sm = std::max(per_sm, 1);
+  // resident CTAs per SM, looked up once per thread and level count
+  thread_local int cached[65] = {};
+  int& per_sm = cached[std::min<uint32_t>(max_levels, 64)];
+  if (per_sm == 0) {
+    EWT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, multi_kernel<T>, kMultiThreads, smem));
+    per_sm = std::max(per_sm, 1);
+  }
   uint32_t const blocks = static_cast<uint32_t>(std::max<uint64_t>(
       1, std::min<uint64_t>(max_items, uint64_t(per_sm) * sm_count())));
   multi_kernel<T><<<blocks, kMultiThreads, smem, s>>>(
@@ -354,6 +484,33 @@ cudaStream_t multi_stream(uint32_t dev) {
 }
 
 }  // namespace
+
+// Loads the serving kernels of one symbol size (module loading is lazy,
+// and the first launch would otherwise pay for it inside a request).
+void prepare_serve_kernels(uint32_t elem_size) {
+  cudaFuncAttributes a{};
+  switch (elem_size) {
+    case 1: EWT_CUDA(cudaFuncGetAttributes(&a, serve_kernel<uint8_t>)); EWT_CUDA(cudaFuncGetAttributes(&a, multi_kernel<uint8_t>)); break;
+    case 2: EWT_CUDA(cudaFuncGetAttributes(&a, serve_kernel<uint16_t>)); EWT_CUDA(cudaFuncGetAttributes(&a, multi_kernel<uint16_t>)); break;
+    case 4: EWT_CUDA(cudaFuncGetAttributes(&a, serve_kernel<uint32_t>)); EWT_CUDA(cudaFuncGetAttributes(&a, multi_kernel<uint32_t>)); break;
+    default: EWT_CUDA(cudaFuncGetAttributes(&a, serve_kernel<uint64_t>)); EWT_CUDA(cudaFuncGetAttributes(&a, multi_kernel<uint64_t>)); break;
+  }
+}
+
+// Zero-copy work-list launch of the serving engine (see ServeReq).
+void launch_serve_items(uint32_t elem_size, TreeView const* d_views,
+                        void const* reqs, void const* items, uint32_t num_items,
+                        uint32_t max_levels, uint32_t* req_err, cudaStream_t s) {
+  if (num_items == 0) return;
+  auto const* r = static_cast<ServeReq const*>(reqs);
+  auto const* it = static_cast<ServeItemD const*>(items);
+  switch (elem_size) {
+    case 1: launch_serve_typed<uint8_t>(d_views, r, it, num_items, max_levels, req_err, s); break;
+    case 2: launch_serve_typed<uint16_t>(d_views, r, it, num_items, max_levels, req_err, s); break;
+    case 4: launch_serve_typed<uint32_t>(d_views, r, it, num_items, max_levels, req_err, s); break;
+    default: launch_serve_typed<uint64_t>(d_views, r, it, num_items, max_levels, req_err, s); break;
+  }
+}
 
 // Work-list launch used by the serving engine: items are already grouped.
 void launch_multi_items(uint32_t elem_size, TreeView const* d_views,

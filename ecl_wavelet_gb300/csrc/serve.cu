@@ -44,10 +44,18 @@ struct ServeItem {  // multi.cu's work item layout
 };
 static_assert(sizeof(ServeItem) == 16, "work item layout");
 
+struct ServeReqH {  // multi.cu's request descriptor layout
+  uint8_t const* types;
+  void const* queries;
+  uint64_t* results;
+  uint32_t tree, pad;
+};
+static_assert(sizeof(ServeReqH) == 32, "request descriptor layout");
+
 struct Slot {
   cudaStream_t st = nullptr;
   cudaEvent_t done = nullptr;
-  PinnedBuf h_q, h_types, h_items, h_out, h_err;
+  PinnedBuf h_q, h_types, h_items, h_out, h_err, h_reqs, h_reqerr;
   DevBuf d_q, d_types, d_items, d_out, d_err;
   std::vector<sched::Request*> reqs;
   std::vector<uint64_t> offs;
@@ -80,6 +88,7 @@ struct ewt_server {
   std::unordered_map<uint64_t, ewt::BuildJob> build_jobs;
   std::thread dispatcher, completer, builder;
   bool stop = false;
+  bool zero_copy = false;  // kernels read requests and write results in place
   std::string fatal;  // set when a worker thread failed
 
   ewt_server(ewt_server_config const& c)
@@ -122,6 +131,42 @@ void dispatcher_loop(ewt_server* S) {
     Slot& sl = S->slots[si];
     sl.reqs = batch;
     sl.offs.clear();
+    if (S->zero_copy) {
+      // descriptors of the callers' buffers; the kernel reads the queries
+      // and writes the results in place
+      auto* reqs = sl.h_reqs.as<ServeReqH>();
+      auto* items = sl.h_items.as<ServeItem>();
+      auto* rerr = sl.h_reqerr.as<uint32_t>();
+      uint32_t nitems = 0;
+      for (size_t i = 0; i < batch.size(); ++i) {
+        sched::Request* r = batch[i];
+        reqs[i] = ServeReqH{r->types, r->queries, r->results, r->tree, 0};
+        rerr[i] = 0;
+        for (uint64_t j = 0; j < r->m; j += kServeChunk)
+          items[nitems++] = ServeItem{static_cast<uint32_t>(i),
+                                      static_cast<uint32_t>(std::min<uint64_t>(kServeChunk, r->m - j)),
+                                      j};
+      }
+      try {
+        launch_serve_items(S->cfg.elem_size, S->views_d, reqs, items, nitems,
+                           S->max_levels, rerr, sl.st);
+        EWT_CUDA(cudaEventRecord(sl.done, sl.st));
+      } catch (std::exception const& e) {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->fatal = e.what();
+        for (auto* r : batch) S->sched.complete(r->id, EWT_ERR_CUDA, now_s());
+        sl.busy = false;
+        S->cv_done.notify_all();
+        S->cv_work.notify_all();
+        continue;
+      }
+      {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->launched.push_back(si);
+      }
+      S->cv_launched.notify_one();
+      continue;
+    }
     uint64_t off = 0;
     uint32_t nitems = 0;
     auto* items = sl.h_items.as<ServeItem>();
@@ -146,6 +191,7 @@ void dispatcher_loop(ewt_server* S) {
                          S->max_levels, sl.d_types.as<uint8_t>(), sl.d_q.get(),
                          sl.d_out.as<uint64_t>(), sl.d_err.as<uint32_t>(), sl.st);
       EWT_CUDA(cudaMemcpyAsync(sl.h_out.get(), sl.d_out.get(), off * 8, cudaMemcpyDeviceToHost, sl.st));
+      EWT_CUDA(cudaMemcpyAsync(sl.h_err.get(), sl.d_err.get(), 4, cudaMemcpyDeviceToHost, sl.st));
       EWT_CUDA(cudaEventRecord(sl.done, sl.st));
     } catch (std::exception const& e) {
       std::lock_guard<std::mutex> lk(S->mu);
@@ -186,17 +232,25 @@ void completer_loop(ewt_server* S) {
     cudaError_t const e = cudaEventSynchronize(sl.done);
     double const t = now_s();
     std::vector<int> status(sl.reqs.size(), EWT_OK);
-    if (e == cudaSuccess) {
+    if (e == cudaSuccess && S->zero_copy) {
+      uint32_t const* rerr = sl.h_reqerr.as<uint32_t>();
+      for (size_t i = 0; i < sl.reqs.size(); ++i)
+        if (rerr[i]) status[i] = EWT_ERR_QUERY;
+    } else if (e == cudaSuccess) {
       uint64_t const* out = sl.h_out.as<uint64_t>();
+      // the batch's invalid-query word says whether any request must be
+      // scanned for the UINT64_MAX results of invalid queries
+      bool const any_bad = *sl.h_err.as<uint32_t>() != 0;
       for (size_t i = 0; i < sl.reqs.size(); ++i) {
         sched::Request* r = sl.reqs[i];
         uint64_t const o = sl.offs[i];
         std::memcpy(r->results, out + o, r->m * 8);
-        for (uint64_t j = 0; j < r->m; ++j)
-          if (r->types[j] != 0 && out[o + j] == UINT64_MAX) {
-            status[i] = EWT_ERR_QUERY;
-            break;
-          }
+        if (any_bad)
+          for (uint64_t j = 0; j < r->m; ++j)
+            if (r->types[j] != 0 && out[o + j] == UINT64_MAX) {
+              status[i] = EWT_ERR_QUERY;
+              break;
+            }
       }
     } else {
       (void)cudaGetLastError();
@@ -293,15 +347,27 @@ extern "C" int ewt_server_create(int gpu_index, const ewt_server_config* cfg,
     EWT_CUDA(cudaMalloc(&S->views_d, kMaxServerTrees * sizeof(TreeView)));
     uint64_t const q = cfg->batch_queries;
     uint64_t const items = q / kServeChunk + cfg->batch_requests + 1;
+    // With pageable-memory access (address translation through the host's
+    // page tables, as on Grace-hosted GPUs) kernels read the callers' query
+    // buffers and write their result buffers in place: no staging copies.
+    int pageable = 0;
+    EWT_CUDA(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, gpu_index));
+    S->zero_copy = pageable == 1 && !cfg->force_staging;
+    prepare_serve_kernels(cfg->elem_size);
     for (uint32_t i = 0; i < cfg->inflight; ++i) S->slots.emplace_back();
     for (auto& sl : S->slots) {
       EWT_CUDA(cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking));
       EWT_CUDA(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming));
+      sl.h_items.ensure(items * sizeof(ServeItem));
+      sl.h_err.ensure(16);
+      if (S->zero_copy) {
+        sl.h_reqs.ensure(cfg->batch_requests * sizeof(ServeReqH));
+        sl.h_reqerr.ensure(cfg->batch_requests * 4);
+        continue;
+      }
       sl.h_q.ensure(q * 16);
       sl.h_types.ensure(q);
-      sl.h_items.ensure(items * sizeof(ServeItem));
       sl.h_out.ensure(q * 8);
-      sl.h_err.ensure(16);
       sl.d_q.alloc(q * 16);
       sl.d_types.alloc(q);
       sl.d_items.alloc(items * sizeof(ServeItem));

@@ -20,7 +20,7 @@ SCHED_LIB_PATH = os.path.join(_PKG, "libewt_sched.so")
 class ServerConfig(C.Structure):
     _fields_ = [("batch_queries", C.c_uint64), ("batch_requests", C.c_uint32),
                 ("inflight", C.c_uint32), ("memory_budget", C.c_uint64),
-                ("elem_size", C.c_uint32)]
+                ("elem_size", C.c_uint32), ("force_staging", C.c_uint32)]
 
 
 class SchedStats(C.Structure):
@@ -91,10 +91,11 @@ class Server:
     """Resident trees + continuous batching of mixed query requests."""
 
     def __init__(self, batch_queries=1 << 20, batch_requests=4096, inflight=2,
-                 memory_budget=200 << 30, elem_size=1, gpu_index=0):
+                 memory_budget=200 << 30, elem_size=1, gpu_index=0,
+                 force_staging=False):
         L = _lib()
         cfg = ServerConfig(batch_queries, batch_requests, inflight, memory_budget,
-                           elem_size)
+                           elem_size, 1 if force_staging else 0)
         self._h = C.c_void_p()
         _check(L.ewt_server_create(gpu_index, C.byref(cfg), C.byref(self._h)),
                "Server")

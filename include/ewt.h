@@ -260,6 +260,10 @@ typedef struct ewt_server_config {
   uint32_t inflight;       /* batches on the GPU at once, 1 .. 8           */
   uint64_t memory_budget;  /* device bytes for resident trees and builds   */
   uint32_t elem_size;      /* symbol size of every tree served             */
+  uint32_t force_staging;  /* 1: stage queries and results through pinned
+                              buffers even when the GPU can read and write
+                              the callers' pageable host buffers in place
+                              (the default there)                         */
 } ewt_server_config;
 int ewt_server_create(int gpu_index, const ewt_server_config* cfg,
                       ewt_server** out);

@@ -29,7 +29,8 @@ def make_requests(rng, trees, texts, alphabets, count):
     return reqs
 
 
-def test_alone_equals_mix(ewt, oracle):
+@pytest.mark.parametrize("staging", [False, True])
+def test_alone_equals_mix(ewt, oracle, staging):
     from ecl_wavelet_gb300.serving import Server
     rng = np.random.default_rng(31)
     texts, alphabets, trees = [], [], []
@@ -39,7 +40,7 @@ def test_alone_equals_mix(ewt, oracle):
         alphabets.append(a)
         trees.append(ewt.WaveletTree(t, a))
     srv = Server(batch_queries=1 << 14, batch_requests=64, inflight=2,
-                 elem_size=1)
+                 elem_size=1, force_staging=staging)
     ids = [srv.add_tree(t) for t in trees]
     reqs = make_requests(rng, trees, texts, alphabets, 120)
     alone = []
@@ -77,12 +78,14 @@ def test_alone_equals_mix(ewt, oracle):
     srv.close()
 
 
-def test_invalid_cancel_and_build(ewt, oracle):
+@pytest.mark.parametrize("staging", [False, True])
+def test_invalid_cancel_and_build(ewt, oracle, staging):
     from ecl_wavelet_gb300.serving import Server
     rng = np.random.default_rng(32)
     t, a = random_text(rng, 100_000, 16, np.uint8)
     tree = ewt.WaveletTree(t, a)
-    srv = Server(batch_queries=1 << 12, batch_requests=8, inflight=1, elem_size=1)
+    srv = Server(batch_queries=1 << 12, batch_requests=8, inflight=1, elem_size=1,
+                 force_staging=staging)
     tid = srv.add_tree(tree)
     good_ty = np.array([1, 2, 0], np.uint8)
     good_q = tree.make_queries([5, 1, 7], [3, 3, 0])
