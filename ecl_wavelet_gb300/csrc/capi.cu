@@ -56,6 +56,29 @@ int guarded(F&& f) {
   }
 }
 
+// Whether kernels on `dev` can read and write pageable host memory
+// (address translation through the host's page tables); looked up once.
+bool pageable_access(int dev) {
+  static std::mutex mu;
+  static int cached[64];
+  static bool init = false;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!init) {
+    for (int& c : cached) c = -1;
+    init = true;
+  }
+  if (dev < 0 || dev >= 64) return false;
+  if (cached[dev] < 0) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+      (void)cudaGetLastError();
+      v = 0;
+    }
+    cached[dev] = v == 1 ? 1 : 0;
+  }
+  return cached[dev] == 1;
+}
+
 // Largest batch moved through the device scratch in one piece.
 constexpr uint64_t kChunk = uint64_t(1) << 25;
 
@@ -126,12 +149,22 @@ int host_batch(ewt_tree* t, void const* in, size_t in_rec, uint8_t const* types,
     std::lock_guard<std::mutex> lk(t->query_mu);
     DeviceGuard g(t->device);
     AllocStream as(t->stream);
+    cudaStream_t s = t->stream;
+    if (pageable_access(t->device)) {
+      // the kernel reads the caller's queries and writes its results in
+      // place (host page tables): no staging copies
+      launch(types, in, m, out, s);
+      int const st = take_query_status(t->err_d, s);
+      if (st != EWT_OK)
+        throw Error(st, "the batch held invalid queries (their results are "
+                        "UINT64_MAX)");
+      return;
+    }
     QueryScratch& sc = t->scratch;
     uint64_t const chunk = std::min(m, kChunk);
     ensure(sc.in, sc.in_cap, chunk * in_rec);
     ensure(sc.out, sc.out_cap, chunk * out_rec);
     if (types) ensure(sc.types, sc.types_cap, chunk);
-    cudaStream_t s = t->stream;
     for (uint64_t b = 0; b < m; b += chunk) {
       uint64_t const k = std::min(chunk, m - b);
       EWT_CUDA(cudaMemcpyAsync(sc.in.get(),
@@ -163,6 +196,14 @@ int rs_host_batch(ewt_rs* r, uint64_t const* in, uint64_t m, uint64_t* out,
     std::lock_guard<std::mutex> lk(r->query_mu);
     DeviceGuard g(r->device);
     AllocStream as(r->stream);
+    if (pageable_access(r->device)) {  // in place, as host_batch
+      launch(in, m, out, r->stream);
+      int const st = take_query_status(r->err_d, r->stream);
+      if (st != EWT_OK)
+        throw Error(st, "the batch held invalid queries (their results are "
+                        "UINT64_MAX)");
+      return;
+    }
     QueryScratch& sc = r->scratch;
     uint64_t const chunk = std::min(m, kChunk);
     ensure(sc.in, sc.in_cap, chunk * 8);
