@@ -53,7 +53,8 @@ def parse():
     p.add_argument("--no-serve", action="store_true",
                    help="skip the serving-loop rate sweep")
     p.add_argument("--cpu-sample", type=int, default=1 << 25)
-    p.add_argument("--only", default="all", choices=["all", "build", "queries"],
+    p.add_argument("--only", default="all",
+                   choices=["all", "build", "queries", "multi", "serve"],
                    help="build: stop after the timed builds; queries: also "
                         "time the query batches (for profiling runs)")
     return p.parse_args()
@@ -395,6 +396,13 @@ def run_ours(args, world, rank, local):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    if args.only in ("multi", "serve"):
+        part = (bench_multi_text(torch, E, dev, gen) if args.only == "multi"
+                else bench_serving(torch, E, dev, gen, text))
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "partial": args.only,
+                              "many_texts" if args.only == "multi" else "serving": part}))
+        return
     for _ in range(args.warmup):
         E.WaveletTree(text, alphabet, gpu_index=local).close()
     clocks = ClockSampler(local)
