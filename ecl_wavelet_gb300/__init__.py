@@ -114,6 +114,8 @@ SIGNATURES = {
     "ewt_last_error": (C.c_char_p, []),
     "ewt_abi_version": (C.c_int, []),
     "ewt_release_cached_memory": (C.c_int, [C.c_int]),
+    "ewt_save": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "ewt_load": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_void_p)]),
     "ewt_build_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_int,
                                   C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
                                   C.c_void_p]),
@@ -294,6 +296,17 @@ class WaveletTree:
         self.info = Info()
         _check(L.ewt_get_info(self._h, C.byref(self.info)), "get_info")
         self.qdtype = QUERY_DTYPE[self.dtype]
+
+    def save(self, path: str):
+        """Writes the index to `path` (ewt_save)."""
+        _check(lib().ewt_save(self._h, os.fsencode(path)), "save")
+
+    @classmethod
+    def load(cls, path: str, gpu_index: int = 0) -> "WaveletTree":
+        """Reads an index written by save() onto a GPU (ewt_load)."""
+        h = C.c_void_p()
+        _check(lib().ewt_load(os.fsencode(path), gpu_index, C.byref(h)), "load")
+        return cls(None, _handle=h.value)
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

@@ -96,6 +96,8 @@ namespace ewt {
 // Host orchestration of one tree build (wt_build.cu).
 void build_tree(ewt_tree& t, const void* data, uint64_t n, int elem_size,
                 const void* alphabet, uint64_t sigma, cudaStream_t stream);
+// Sets t.view from the tree's device buffers and shape (wt_build.cu).
+void fill_tree_view(ewt_tree& t);
 
 // Query launches on device buffers (queries.cu).
 void launch_access(ewt_tree& t, const uint64_t* d_idx, uint64_t m,

@@ -619,24 +619,8 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   EWT_CUDA(cudaStreamSynchronize(st));  // host vectors above leave scope
 
   t.n = n;
+  fill_tree_view(t);
   TreeView& v = t.view;
-  v.rs = t.rs.view();
-  v.counts = t.counts_d.as<uint64_t>();
-  v.node_ranks = t.ranks_d.as<uint64_t>();
-  v.node_base = t.node_base_d.as<uint64_t>();
-  v.nodes_at_level = t.nodes_at_level_d.as<uint64_t>();
-  v.code_len = t.code_len_d.as<uint64_t>();
-  v.code_bits = t.code_bits_d.as<uint64_t>();
-  v.alphabet = t.is_min ? nullptr : t.alphabet_d.get();
-  v.n = n;
-  v.sigma = sigma;
-  v.codes_start = t.codes_start;
-  v.num_ranks = t.nodes.size();
-  v.num_nodes_until_last_level = t.nodes_until_last;
-  v.levels = L;
-  v.elem_size = sizeof(T);
-  v.is_pow2 = t.pow2;
-  v.is_min = t.is_min;
 
   // ---- level 0 bits
   uint32_t* const words = t.rs.words.as<uint32_t>();
@@ -734,6 +718,27 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
 }
 
 }  // namespace
+
+void fill_tree_view(ewt_tree& t) {
+  TreeView& v = t.view;
+  v.rs = t.rs.view();
+  v.counts = t.counts_d.as<uint64_t>();
+  v.node_ranks = t.ranks_d.as<uint64_t>();
+  v.node_base = t.node_base_d.as<uint64_t>();
+  v.nodes_at_level = t.nodes_at_level_d.as<uint64_t>();
+  v.code_len = t.code_len_d.as<uint64_t>();
+  v.code_bits = t.code_bits_d.as<uint64_t>();
+  v.alphabet = t.is_min ? nullptr : t.alphabet_d.get();
+  v.n = t.n;
+  v.sigma = t.sigma;
+  v.codes_start = t.codes_start;
+  v.num_ranks = t.nodes.size();
+  v.num_nodes_until_last_level = t.nodes_until_last;
+  v.levels = t.L;
+  v.elem_size = t.elem_size;
+  v.is_pow2 = t.pow2;
+  v.is_min = t.is_min;
+}
 
 void build_tree(ewt_tree& t, const void* data, uint64_t n, int elem_size,
                 const void* alphabet, uint64_t sigma, cudaStream_t stream) {

@@ -215,6 +215,14 @@ int ewt_abi_version(void);
 /* Number of kernel launches this library issued since load (all threads). */
 uint64_t ewt_launch_count(void);
 
+/* ---- index files --------------------------------------------------------
+ * Writes a built tree (shape, level bits, RankSelect counts and samples,
+ * rank blocks, count table, node ranks) to `path`; ewt_load reads it back
+ * onto a GPU without rebuilding.  Files are native-endian and versioned by
+ * their magic.  No reference counterpart (the reference rebuilds). */
+int ewt_save(const ewt_tree* tree, const char* path);
+int ewt_load(const char* path, int gpu_index, ewt_tree** out);
+
 /* ---- many trees at once ------------------------------------------------
  * Builds `count` texts (elem_size bytes per symbol) concurrently, each on its
  * own stream: out[i] receives tree i (NULL when its build failed, with

@@ -97,3 +97,27 @@ def test_pool_reuse_and_release(ewt, oracle):
         gt.close()
         if i == 1:
             ewt.release_cached_memory(0)
+
+
+@pytest.mark.parametrize("dtype,sigma,minimal", [(np.uint8, 256, True),
+                                                 (np.uint16, 1000, False),
+                                                 (np.uint64, 12, False)])
+def test_save_load_round_trip(ewt, oracle, tmp_path, dtype, sigma, minimal):
+    """An index written by save() and read back by load() exports the same
+    structures and answers the same queries without a rebuild."""
+    from tests.workloads import random_text
+    rng = np.random.default_rng(sigma)
+    text, alphabet = random_text(rng, 250_000, sigma, dtype, minimal=minimal)
+    gt = ewt.WaveletTree(text, alphabet)
+    path = str(tmp_path / "index.ewt")
+    gt.save(path)
+    lt = ewt.WaveletTree.load(path)
+    ot = oracle.OracleTree(text, alphabet)
+    assert_same_tree(lt, ot)
+    al = np.asarray(alphabet, dtype=np.uint64)
+    check_queries(lt, ot, text, al, 5_000, seed=4)
+    lt.close()
+    with open(path, "r+b") as f:  # a damaged file is refused, not loaded
+        f.write(b"NOTANIDX")
+    with pytest.raises(ewt.EwtError):
+        ewt.WaveletTree.load(path)
