@@ -52,9 +52,11 @@ def parse():
                    help="skip the many-text build and multi-tree queries")
     p.add_argument("--no-serve", action="store_true",
                    help="skip the serving-loop rate sweep")
+    p.add_argument("--no-rs", action="store_true",
+                   help="skip the standalone RankSelect comparison")
     p.add_argument("--cpu-sample", type=int, default=1 << 25)
     p.add_argument("--only", default="all",
-                   choices=["all", "build", "queries", "multi", "serve"],
+                   choices=["all", "build", "queries", "multi", "serve", "rs"],
                    help="build: stop after the timed builds; queries: also "
                         "time the query batches (for profiling runs)")
     return p.parse_args()
@@ -356,6 +358,81 @@ def bench_serving(torch, E, dev, gen, big_text):
             "sweep": out}
 
 
+def bench_rank_select(torch, E, dev, seed=11):
+    """Standalone RankSelect (ecl::RankSelect): one 2^32-bit array of iid
+    bits; build from device words and 2^26 rank and select queries (host
+    buffers, answered in place) on the GPU, next to the CPU restatement
+    (popcount rank / sampled select, one query per iteration on all host
+    cores) on 2^24 queries of the same array."""
+    import ctypes
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    bits = 1 << 32
+    words = rng.integers(0, 1 << 32, bits // 32, dtype=np.uint64).astype(np.uint32)
+    d_words = torch.from_numpy(words.view(np.int32)).to(dev)
+    bits_arr = np.array([bits], dtype=np.uint64)
+    L = E.lib()
+
+    def gpu_build():
+        h = ctypes.c_void_p()
+        st = L.ewt_rs_build(ctypes.c_void_p(d_words.data_ptr()),
+                            bits_arr.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                            1, 0, ctypes.byref(h))
+        assert st == 0
+        return h
+
+    L.ewt_rs_free(gpu_build())
+    torch.cuda.synchronize()
+    a = time.perf_counter()
+    h = gpu_build()
+    build_s = time.perf_counter() - a
+    rs = E.RankSelect.__new__(E.RankSelect)
+    rs._h, rs.bits = h, bits_arr
+    ones = int(rs.export("TOTAL_ONES")[0])
+    m = 1 << 26
+    pos = rng.integers(0, bits + 1, m, dtype=np.uint64)
+    ks = rng.integers(1, ones + 1, m, dtype=np.uint64)
+    # result buffers written once before timing (allocation, not queries)
+    r_gpu = np.zeros(m, dtype=np.uint64)
+    s_gpu = np.zeros(m, dtype=np.uint64)
+    rs.rank(0, 1, pos, out=r_gpu)
+    rs.select(0, 1, ks, out=s_gpu)
+    a = time.perf_counter()
+    rs.rank(0, 1, pos, out=r_gpu)
+    rank_s = time.perf_counter() - a
+    a = time.perf_counter()
+    rs.select(0, 1, ks, out=s_gpu)
+    sel_s = time.perf_counter() - a
+    # the same call into a freshly allocated result array (the library
+    # populates its pages before the GPU writes them)
+    a = time.perf_counter()
+    fresh = rs.rank(0, 1, pos)
+    fresh_s = time.perf_counter() - a
+    assert np.array_equal(fresh, r_gpu)
+    rs.close()
+    a = time.perf_counter()
+    ors = O.OracleRS([words], [bits])
+    cpu_build_s = time.perf_counter() - a
+    mc = 1 << 24
+    a = time.perf_counter()
+    r_cpu = ors.rank_batch(0, pos[:mc], 1)
+    cpu_rank_s = time.perf_counter() - a
+    a = time.perf_counter()
+    s_cpu = ors.select_batch(0, ks[:mc], 1)
+    cpu_sel_s = time.perf_counter() - a
+    assert np.array_equal(r_gpu[:mc], r_cpu) and np.array_equal(s_gpu[:mc], s_cpu)
+    cores = int(O.lib().ewto_max_threads())
+    return {"bits": bits, "queries": m,
+            "gpu_build_GB_s": bits / 8 / build_s / 1e9,
+            "gpu_rank_Mq_s": m / rank_s / 1e6, "gpu_select_Mq_s": m / sel_s / 1e6,
+            "gpu_rank_fresh_output_Mq_s": m / fresh_s / 1e6,
+            "cpu_cores": cores, "cpu_build_GB_s": bits / 8 / cpu_build_s / 1e9,
+            "cpu_rank_Mq_s": mc / cpu_rank_s / 1e6,
+            "cpu_select_Mq_s": mc / cpu_sel_s / 1e6,
+            "rank_gpu_over_cpu": (m / rank_s) / (mc / cpu_rank_s),
+            "select_gpu_over_cpu": (m / sel_s) / (mc / cpu_sel_s)}
+
+
 def make_mixed_queries(torch, tree, n, sigma, m, gen):
     """Device-resident mixed batch: types 40/40/20, RankSelectQuery records."""
     dev = "cuda"
@@ -396,12 +473,15 @@ def run_ours(args, world, rank, local):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    if args.only in ("multi", "serve"):
-        part = (bench_multi_text(torch, E, dev, gen) if args.only == "multi"
-                else bench_serving(torch, E, dev, gen, text))
+    if args.only in ("multi", "serve", "rs"):
+        if args.only == "multi":
+            key, part = "many_texts", bench_multi_text(torch, E, dev, gen)
+        elif args.only == "serve":
+            key, part = "serving", bench_serving(torch, E, dev, gen, text)
+        else:
+            key, part = "rank_select", bench_rank_select(torch, E, dev)
         if rank == 0:
-            print(json.dumps({"metric": METRIC, "partial": args.only,
-                              "many_texts" if args.only == "multi" else "serving": part}))
+            print(json.dumps({"metric": METRIC, "partial": args.only, key: part}))
         return
     for _ in range(args.warmup):
         E.WaveletTree(text, alphabet, gpu_index=local).close()
@@ -596,6 +676,9 @@ def run_ours(args, world, rank, local):
         multi = bench_multi_text(torch, E, dev, gen)
     if not args.no_serve:
         serve = bench_serving(torch, E, dev, gen, text)
+    rsel = None
+    if not args.no_rs and rank == 0 and world == 1:
+        rsel = bench_rank_select(torch, E, dev)
 
     # ---- CPU baseline (rank 0, N = 1 only) ---------------------------------
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -635,7 +718,7 @@ def run_ours(args, world, rank, local):
             "gpu_launches": launches,
             "roofline": roofline, "build": build, "queries": queries,
             "sigma_sweep_GB_s": sweep, "e2e": e2e, "cpu_baseline": cpu,
-            "many_texts": multi, "serving": serve,
+            "many_texts": multi, "serving": serve, "rank_select": rsel,
             "clocks": clk,
         }
         print(json.dumps(line))

@@ -463,16 +463,21 @@ class RankSelect:
                                    C.byref(size)), "export")
         return out
 
-    def rank(self, array: int, value: int, pos) -> np.ndarray:
+    def rank(self, array: int, value: int, pos, out=None) -> np.ndarray:
+        """rank_value of every position; `out` (uint64, reused when given)
+        receives the results."""
         p = np.ascontiguousarray(pos, dtype=np.uint64)
-        out = np.zeros(p.size, dtype=np.uint64)
+        if out is None:
+            out = np.zeros(p.size, dtype=np.uint64)
         _check(lib().ewt_rs_rank(self._h, array, value, _ptr(p), p.size,
                                  _ptr(out)), "rs_rank")
         return out
 
-    def select(self, array: int, value: int, i) -> np.ndarray:
+    def select(self, array: int, value: int, i, out=None) -> np.ndarray:
+        """select_value of every index (1-based); `out` as for rank()."""
         p = np.ascontiguousarray(i, dtype=np.uint64)
-        out = np.zeros(p.size, dtype=np.uint64)
+        if out is None:
+            out = np.zeros(p.size, dtype=np.uint64)
         _check(lib().ewt_rs_select(self._h, array, value, _ptr(p), p.size,
                                    _ptr(out)), "rs_select")
         return out

@@ -11,6 +11,11 @@
 #include <new>
 #include <string>
 
+#ifdef __linux__
+#include <sys/mman.h>
+#include <unistd.h>
+#endif
+
 #include "internal.cuh"
 
 namespace ewt {
@@ -77,6 +82,38 @@ bool pageable_access(int dev) {
     cached[dev] = v == 1 ? 1 : 0;
   }
   return cached[dev] == 1;
+}
+
+// Result buffers the GPU will write in place: pageable pages that were never
+// touched would be populated one GPU-initiated fault at a time (tens of
+// times slower than the batch itself), so a buffer whose first or last page
+// is not resident is populated from the host first.  Pinned or registered
+// memory, and buffers already in use, are left alone.
+void populate_for_write(void* p, size_t bytes) {
+#ifdef __linux__
+#ifndef MADV_POPULATE_WRITE
+#define MADV_POPULATE_WRITE 23
+#endif
+  if (!p || bytes == 0) return;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return;
+  }
+  if (a.type != cudaMemoryTypeUnregistered) return;
+  uintptr_t const page = static_cast<uintptr_t>(sysconf(_SC_PAGESIZE));
+  uintptr_t const b = reinterpret_cast<uintptr_t>(p) & ~(page - 1);
+  uintptr_t const e = reinterpret_cast<uintptr_t>(p) + bytes;
+  uintptr_t const last = (e - 1) & ~(page - 1);
+  unsigned char r0 = 0, r1 = 0;
+  if (mincore(reinterpret_cast<void*>(b), 1, &r0) == 0 &&
+      mincore(reinterpret_cast<void*>(last), 1, &r1) == 0 && (r0 & 1) && (r1 & 1))
+    return;
+  (void)madvise(reinterpret_cast<void*>(b), e - b, MADV_POPULATE_WRITE);
+#else
+  (void)p;
+  (void)bytes;
+#endif
 }
 
 // Largest batch moved through the device scratch in one piece.
@@ -153,6 +190,7 @@ int host_batch(ewt_tree* t, void const* in, size_t in_rec, uint8_t const* types,
     if (pageable_access(t->device)) {
       // the kernel reads the caller's queries and writes its results in
       // place (host page tables): no staging copies
+      populate_for_write(out, m * out_rec);
       launch(types, in, m, out, s);
       int const st = take_query_status(t->err_d, s);
       if (st != EWT_OK)
@@ -197,6 +235,7 @@ int rs_host_batch(ewt_rs* r, uint64_t const* in, uint64_t m, uint64_t* out,
     DeviceGuard g(r->device);
     AllocStream as(r->stream);
     if (pageable_access(r->device)) {  // in place, as host_batch
+      populate_for_write(out, m * 8);
       launch(in, m, out, r->stream);
       int const st = take_query_status(r->err_d, r->stream);
       if (st != EWT_OK)

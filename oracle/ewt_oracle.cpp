@@ -792,6 +792,22 @@ uint64_t ewto_rs_select(void* h, int array, uint64_t i, int value) {
   return s->arrays[array].select(i, value);
 }
 
+// Batches of binary rank / select on all host threads (the CPU popcount
+// baseline of the standalone RankSelect; one query per loop iteration).
+void ewto_rs_rank_batch(void* h, int array, const uint64_t* pos, uint64_t m,
+                        int value, uint64_t* out, int nthreads) {
+  auto& b = static_cast<RSSet*>(h)->arrays[array];
+#pragma omp parallel for schedule(static) num_threads(nthreads_or_max(nthreads))
+  for (int64_t i = 0; i < static_cast<int64_t>(m); ++i) out[i] = b.rank(pos[i], value);
+}
+
+void ewto_rs_select_batch(void* h, int array, const uint64_t* idx, uint64_t m,
+                          int value, uint64_t* out, int nthreads) {
+  auto& b = static_cast<RSSet*>(h)->arrays[array];
+#pragma omp parallel for schedule(static) num_threads(nthreads_or_max(nthreads))
+  for (int64_t i = 0; i < static_cast<int64_t>(m); ++i) out[i] = b.select(idx[i], value);
+}
+
 int ewto_minimal_codes(uint64_t sigma, uint64_t* lens, uint64_t* codes,
                        uint64_t cap, uint64_t* count) {
   if (sigma < 2) return EWT_ERR_INVALID_ARGUMENT;

@@ -61,6 +61,10 @@ int ewto_rs_export(void* h, int component, int array, void* buf,
                    uint64_t cap_bytes, uint64_t* size_bytes);
 uint64_t ewto_rs_rank(void* h, int array, uint64_t pos, int value);
 uint64_t ewto_rs_select(void* h, int array, uint64_t i, int value);
+void ewto_rs_rank_batch(void* h, int array, const uint64_t* pos, uint64_t m,
+                        int value, uint64_t* out, int nthreads);
+void ewto_rs_select_batch(void* h, int array, const uint64_t* idx, uint64_t m,
+                          int value, uint64_t* out, int nthreads);
 
 /* Alphabet-shape helpers used by the known-answer tests. */
 int ewto_minimal_codes(uint64_t sigma, uint64_t* lens, uint64_t* codes,

@@ -89,6 +89,11 @@ def lib():
         L.ewto_rs_rank.restype = C.c_uint64
         L.ewto_rs_select.argtypes = [C.c_void_p, C.c_int, C.c_uint64, C.c_int]
         L.ewto_rs_select.restype = C.c_uint64
+        for name in ("ewto_rs_rank_batch", "ewto_rs_select_batch"):
+            f = getattr(L, name)
+            f.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_uint64, C.c_int,
+                          C.c_void_p, C.c_int]
+            f.restype = None
         L.ewto_minimal_codes.argtypes = [C.c_uint64, u64p, u64p, C.c_uint64,
                                          u64p]
         L.ewto_node_infos.argtypes = [C.c_uint64, u64p, u64p, C.c_uint64, u64p]
@@ -232,6 +237,20 @@ class OracleRS:
 
     def select(self, array, i, value):
         return lib().ewto_rs_select(self.h, array, i, value)
+
+    def rank_batch(self, array, pos, value, nthreads=0):
+        pos = _u64(pos)
+        out = np.empty(pos.size, dtype=np.uint64)
+        lib().ewto_rs_rank_batch(self.h, array, pos.ctypes.data, pos.size, value,
+                                 out.ctypes.data, nthreads)
+        return out
+
+    def select_batch(self, array, idx, value, nthreads=0):
+        idx = _u64(idx)
+        out = np.empty(idx.size, dtype=np.uint64)
+        lib().ewto_rs_select_batch(self.h, array, idx.ctypes.data, idx.size, value,
+                                   out.ctypes.data, nthreads)
+        return out
 
 
 def minimal_codes(sigma: int):
