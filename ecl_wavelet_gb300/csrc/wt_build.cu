@@ -152,6 +152,102 @@ __global__ void presence_kernel(T const* __restrict__ text, uint64_t n,
     if (sm[i]) atomicOr(&bitmap[i], sm[i]);
 }
 
+// Alphabet detection for 4- and 8-byte symbols: a device hash set of the
+// distinct symbols (open addressing, linear probing, 64-bit slots).  An
+// empty slot holds kEmptySlot; for 8-byte texts the one symbol equal to it is
+// recorded in a flag instead.  A symbol is looked up with a plain load first
+// (most symbols repeat) and inserted with atomicCAS only when missing; warp
+// peers holding the same symbol insert once.  A probe that runs around the
+// whole table reports overflow and the host retries with a larger table.
+constexpr uint64_t kEmptySlot = ~uint64_t(0);
+
+__device__ __forceinline__ uint64_t slot_hash(uint64_t x) {
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdull;
+  x ^= x >> 33;
+  return x;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256)
+distinct_kernel(T const* __restrict__ text, uint64_t n,
+                unsigned long long* __restrict__ table, uint64_t cap_mask,
+                unsigned long long* __restrict__ count,
+                uint32_t* __restrict__ flags) {  // [0] overflow, [1] max symbol seen
+  uint64_t const stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n;
+       i += stride) {
+    uint64_t const key = static_cast<uint64_t>(text[i]);
+    uint32_t const peers = __match_any_sync(__activemask(), key);
+    if ((threadIdx.x & 31) != __ffs(peers) - 1) continue;  // one per value
+    if (key == kEmptySlot) {
+      flags[1] = 1;
+      continue;
+    }
+    uint64_t h = slot_hash(key) & cap_mask;
+    for (uint64_t probe = 0;; ++probe) {
+      if (probe > cap_mask) {
+        flags[0] = 1;
+        break;
+      }
+      uint64_t const cur = table[h];
+      if (cur == key) break;
+      if (cur == kEmptySlot) {
+        unsigned long long const prev =
+            atomicCAS(&table[h], static_cast<unsigned long long>(kEmptySlot),
+                      static_cast<unsigned long long>(key));
+        if (prev == kEmptySlot) {
+          atomicAdd(count, 1ull);
+          break;
+        }
+        if (prev == key) break;
+      }
+      h = (h + 1) & cap_mask;
+    }
+  }
+}
+
+// Sorted distinct symbols of a device-resident 4- or 8-byte text.
+template <class T>
+std::vector<uint64_t> detect_alphabet_wide(T const* d_text, uint64_t n,
+                                           cudaStream_t st) {
+  uint64_t cap = 1ull << 16;
+  uint32_t const blocks = static_cast<uint32_t>(
+      std::min<uint64_t>(ceil_div(n, 256), uint64_t(sm_count()) * 8));
+  for (;;) {
+    DevBuf table(cap * 8), cnt(8), flags(8);
+    EWT_CUDA(cudaMemsetAsync(table.get(), 0xFF, cap * 8, st));
+    EWT_CUDA(cudaMemsetAsync(cnt.get(), 0, 8, st));
+    EWT_CUDA(cudaMemsetAsync(flags.get(), 0, 8, st));
+    distinct_kernel<T><<<blocks, 256, 0, st>>>(
+        d_text, n, table.as<unsigned long long>(), cap - 1,
+        cnt.as<unsigned long long>(), flags.as<uint32_t>());
+    EWT_LAUNCHED();
+    uint64_t count = 0;
+    uint32_t fl[2] = {0, 0};
+    EWT_CUDA(cudaMemcpyAsync(&count, cnt.get(), 8, cudaMemcpyDeviceToHost, st));
+    EWT_CUDA(cudaMemcpyAsync(fl, flags.get(), 8, cudaMemcpyDeviceToHost, st));
+    EWT_CUDA(cudaStreamSynchronize(st));
+    if (!fl[0] && count * 2 <= cap) {
+      std::vector<uint64_t> h(cap);
+      EWT_CUDA(cudaMemcpyAsync(h.data(), table.get(), cap * 8,
+                               cudaMemcpyDeviceToHost, st));
+      EWT_CUDA(cudaStreamSynchronize(st));
+      std::vector<uint64_t> out;
+      out.reserve(count + 1);
+      for (uint64_t v : h)
+        if (v != kEmptySlot) out.push_back(v);
+      if (fl[1]) out.push_back(kEmptySlot);
+      std::sort(out.begin(), out.end());
+      return out;
+    }
+    // table too small: at least four times the symbols seen so far
+    uint64_t want = std::max(cap * 2, count * 4);
+    cap = 1;
+    while (cap < want) cap <<= 1;
+  }
+}
+
 // Text -> minimal symbols (lower_bound in the sorted alphabet).
 template <class T>
 __global__ void __launch_bounds__(256)
@@ -471,13 +567,7 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
       for (uint64_t v = 0; v < kWords * 32ull; ++v)
         if ((h[v >> 5] >> (v & 31)) & 1) t.alphabet.push_back(v);
     } else {
-      std::vector<T> host(n);
-      EWT_CUDA(cudaMemcpyAsync(host.data(), d_text, n * sizeof(T),
-                               cudaMemcpyDeviceToHost, st));
-      EWT_CUDA(cudaStreamSynchronize(st));
-      std::sort(host.begin(), host.end());
-      host.erase(std::unique(host.begin(), host.end()), host.end());
-      t.alphabet.assign(host.begin(), host.end());
+      t.alphabet = detect_alphabet_wide<T>(d_text, n, st);
     }
   } else {
     T const* a = static_cast<T const*>(alphabet);

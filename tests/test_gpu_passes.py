@@ -121,3 +121,21 @@ def test_save_load_round_trip(ewt, oracle, tmp_path, dtype, sigma, minimal):
         f.write(b"NOTANIDX")
     with pytest.raises(ewt.EwtError):
         ewt.WaveletTree.load(path)
+
+
+@pytest.mark.parametrize("dtype,sigma", [(np.uint32, 40_000), (np.uint64, 300)])
+def test_detected_wide_alphabet(ewt, oracle, dtype, sigma):
+    """Alphabets of 4- and 8-byte texts detected on the GPU (hash set) equal
+    the oracle's, including the extreme values 0 and the type's maximum."""
+    rng = np.random.default_rng(sigma)
+    info = np.iinfo(dtype)
+    vals = np.unique(rng.integers(0, info.max, sigma * 2, dtype=np.uint64).astype(dtype))
+    vals = vals[:sigma - 2]
+    vals = np.unique(np.concatenate([vals, np.array([0, info.max], dtype=dtype)]))
+    text = vals[rng.integers(0, vals.size, 400_000)]
+    text[:vals.size] = vals  # every symbol present
+    gt = ewt.WaveletTree(text)  # alphabet detected
+    ot = oracle.OracleTree(text)
+    assert np.array_equal(gt.getAlphabet(), np.sort(vals))
+    assert_same_tree(gt, ot)
+    check_queries(gt, ot, text, np.sort(vals).astype(np.uint64), 3_000, seed=6)
