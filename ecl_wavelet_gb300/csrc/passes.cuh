@@ -39,7 +39,7 @@ constexpr uint32_t kPChunk = 65536;               // symbols per chunk
 constexpr uint32_t kPMaxK = 4;                     // levels per pass
 constexpr uint32_t kPMaxDigits = 1u << kPMaxK;
 constexpr uint32_t kPMaxStartLevel = 12;           // <= 4096 nodes per pass
-constexpr uint32_t kPStages = 3;
+constexpr uint32_t kPStages = 2;
 
 struct PassArgs {
   uint64_t n;
@@ -354,7 +354,7 @@ __device__ __forceinline__ uint32_t bits_from(uint32_t const* buf, int32_t s0) {
 // 4. The pass kernel.  Persistent: CTA b takes chunks b, b + G, ...; tiles
 //    of a chunk in order (running class counts carry from tile to tile).
 template <class T, bool WriteOrder>
-__global__ void __launch_bounds__(kPThreads, 4)
+__global__ void __launch_bounds__(kPThreads, 5)
 pass_kernel(T const* __restrict__ src, T* __restrict__ dst, PassArgs p) {
   using Shape = PassShape<T>;
   constexpr uint32_t kItems = Shape::kItems;

@@ -494,7 +494,7 @@ void run_passes(ewt_tree& t, T const* sym, uint64_t n, uint32_t* err,
       next = ob.as<T>();
     }
     uint32_t const grid = static_cast<uint32_t>(
-        std::min<uint64_t>(max_chunks, uint64_t(sms) * 4));
+        std::min<uint64_t>(max_chunks, uint64_t(sms) * 5));
     {
       PhaseTimer pt(EWT_PHASE_HIST, st);
       chunk_table_kernel<<<1, 1024, 0, st>>>(pa);
