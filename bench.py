@@ -613,7 +613,23 @@ def run_ours(args, world, rank, local):
         assert st == 0
 
     e2e_q_ms = timed(host_mixed, reps=2)
+    # launch shapes picked by the library's autotuner, then the same calls
+    tuning = tree.autotune(1 << 22)
+    tuned_mixed_ms = timed(lambda: tree.mixed_device(
+        types.data_ptr(), rec.data_ptr(), m, out.data_ptr(), sptr))
+    tuned_plain_ms = (
+        timed(lambda: tree.access_device(acc_idx.data_ptr(), acc_idx.numel(),
+                                         o_acc.data_ptr(), sptr))
+        + timed(lambda: tree.rank_device(rq.data_ptr(), rq.shape[0],
+                                         o_r.data_ptr(), sptr))
+        + timed(lambda: tree.select_device(sq.data_ptr(), sq.shape[0],
+                                           o_s.data_ptr(), sptr)))
+    assert tree.query_status(sptr) == 0
     queries = {
+        "autotuned": {"shapes": {k: [v["threads"], v["blocks_per_sm"]]
+                                 for k, v in tuning.items()},
+                      "batched_mixed_Mq_s": m / tuned_mixed_ms / 1e3,
+                      "plain_per_type_Mq_s": m / tuned_plain_ms / 1e3},
         "n_queries": m, "mix": "40/40/20 access/rank/select, interleaved",
         "batched_mixed_Mq_s": m / mixed_ms / 1e3,
         "plain_per_type_Mq_s": m / plain_ms / 1e3,

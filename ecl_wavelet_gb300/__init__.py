@@ -67,6 +67,13 @@ class Info(C.Structure):
                 ("device_bytes", C.c_uint64)]
 
 
+class Tuning(C.Structure):
+    """Launch shapes chosen by ewt_autotune per query kind (access, rank,
+    select, mixed) and the probe rates they gave."""
+    _fields_ = [("threads", C.c_uint32 * 4), ("blocks_per_sm", C.c_uint32 * 4),
+                ("default_mq_s", C.c_double * 4), ("tuned_mq_s", C.c_double * 4)]
+
+
 # Every symbol libewt.so exports, with its ctypes signature.
 _U64P = C.POINTER(C.c_uint64)
 SIGNATURES = {
@@ -125,6 +132,7 @@ SIGNATURES = {
     "ewt_mixed_multi_device": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p,
                                          C.c_void_p, C.c_void_p, C.c_uint64,
                                          C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ewt_autotune": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Tuning)]),
     "ewt_launch_count": (C.c_uint64, []),
     "ewt_set_timing": (None, [C.c_int]),
     "ewt_get_timing": (None, [C.c_void_p, C.c_int]),
@@ -307,6 +315,20 @@ class WaveletTree:
         h = C.c_void_p()
         _check(lib().ewt_load(os.fsencode(path), gpu_index, C.byref(h)), "load")
         return cls(None, _handle=h.value)
+
+    def autotune(self, probe_queries: int = 1 << 22) -> dict:
+        """Times the query kernels on `probe_queries` device-generated valid
+        queries per kind for candidate launch shapes and keeps the fastest
+        for every later query on this tree (ewt_autotune).  Returns, per
+        kind, the chosen threads per CTA, resident CTAs per SM (0 = as many
+        as fit) and the default and tuned rates in million queries/s."""
+        tu = Tuning()
+        _check(lib().ewt_autotune(self._h, probe_queries, C.byref(tu)), "autotune")
+        return {kind: {"threads": tu.threads[i],
+                       "blocks_per_sm": tu.blocks_per_sm[i],
+                       "default_mq_s": tu.default_mq_s[i],
+                       "tuned_mq_s": tu.tuned_mq_s[i]}
+                for i, kind in enumerate(("access", "rank", "select", "mixed"))}
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

@@ -672,6 +672,19 @@ void ewt_get_timing(ewt_phase_times* out, int reset) {
 const char* ewt_last_error(void) { return g_last_error.c_str(); }
 int ewt_abi_version(void) { return EWT_ABI_VERSION; }
 
+int ewt_autotune(ewt_tree* t, uint64_t probe_queries, ewt_tuning* out) {
+  return guarded([&] {
+    EWT_REQUIRE(t != nullptr, EWT_ERR_INVALID_ARGUMENT, "tree is null");
+    EWT_REQUIRE(probe_queries >= 1024 && probe_queries <= (uint64_t(1) << 28),
+                EWT_ERR_INVALID_ARGUMENT, "probe_queries must be in [2^10, 2^28]");
+    std::lock_guard<std::mutex> lk(t->query_mu);
+    DeviceGuard g(t->device);
+    AllocStream as(t->stream);
+    if (out) std::memset(out, 0, sizeof(*out));
+    autotune_queries(*t, probe_queries, out);
+  });
+}
+
 int ewt_release_cached_memory(int gpu_index) {
   return guarded([&] {
     DeviceGuard g(gpu_index);

@@ -63,6 +63,10 @@ struct NodeInfoH {
 struct ewt_tree {
   int device = 0;
   uint32_t elem_size = 1;
+  // query launch shape per kind (access, rank, select, mixed) chosen by
+  // ewt_autotune: threads per CTA and resident CTAs per SM (0 = default)
+  uint32_t tune_threads[4] = {0, 0, 0, 0};
+  uint32_t tune_blocks[4] = {0, 0, 0, 0};
   uint64_t n = 0, sigma = 0;
   uint32_t L = 0;
   bool is_min = false, pow2 = false;
@@ -130,6 +134,9 @@ void launch_serve_items(uint32_t elem_size, TreeView const* d_views,
                         void const* reqs, void const* items, uint32_t num_items,
                         uint32_t max_levels, uint32_t* req_err, cudaStream_t s);
 void prepare_serve_kernels(uint32_t elem_size);
+// Times candidate launch shapes of every query kind on probe queries and
+// keeps the fastest in the tree (queries.cu).
+void autotune_queries(ewt_tree& t, uint64_t probe_queries, ewt_tuning* out);
 void launch_rs_rank(ewt_rs& r, int array, int value, const uint64_t* d_pos,
                     uint64_t m, uint64_t* d_out, cudaStream_t s);
 void launch_rs_select(ewt_rs& r, int array, int value, const uint64_t* d_i,

@@ -27,7 +27,8 @@ static_assert(sizeof(QueryRec<uint64_t>) == 16, "RankSelectQuery layout");
 
 enum Kind { kAccess = 0, kRank = 1, kSelect = 2, kMixed = 3 };
 
-constexpr uint32_t kQueryThreads = 256;
+constexpr uint32_t kQueryThreads = 256;     // default threads per CTA
+constexpr uint32_t kMaxQueryThreads = 256;  // largest the autotuner tries
 // Staging budget per CTA: small enough that 8 CTAs (2048 threads) fit on an
 // SM's 228 KB of shared memory.
 constexpr uint64_t kStageLimitBytes = 24 * 1024;
@@ -54,7 +55,7 @@ inline StagePlan plan_stage(ewt_tree const& t) {
 }
 
 template <class T, int K>
-__global__ void __launch_bounds__(kQueryThreads)
+__global__ void __launch_bounds__(kMaxQueryThreads)
 query_kernel(TreeView t, uint8_t const* __restrict__ types,
              void const* __restrict__ in, uint64_t m, void* __restrict__ out,
              uint32_t* __restrict__ err, uint32_t stage_counts,
@@ -144,7 +145,7 @@ query_kernel(TreeView t, uint8_t const* __restrict__ types,
 constexpr uint32_t kMixChunk = 2048;
 
 template <class T>
-__global__ void __launch_bounds__(kQueryThreads)
+__global__ void __launch_bounds__(kMaxQueryThreads)
 mixed_kernel(TreeView t, uint8_t const* __restrict__ types,
              QueryRec<T> const* __restrict__ in, uint64_t m,
              uint64_t* __restrict__ out, uint32_t* __restrict__ err,
@@ -302,15 +303,17 @@ void launch_typed(ewt_tree& t, uint8_t const* types, void const* in,
           static_cast<int>(kStageLimitBytes + 4096)));
       mattr[mi] = true;
     }
+    uint32_t const threads = t.tune_threads[K] ? t.tune_threads[K] : kQueryThreads;
     int per_sm = 0;
     EWT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mk,
-                                                           kQueryThreads, p.bytes));
+                                                           threads, p.bytes));
     per_sm = std::max(per_sm, 1);
+    if (t.tune_blocks[K]) per_sm = std::min<int>(per_sm, t.tune_blocks[K]);
     uint64_t const chunks = ceil_div(m, kMixChunk);
     uint32_t const blocks = static_cast<uint32_t>(
         std::min<uint64_t>(chunks, uint64_t(per_sm) * sm_count()));
     PhaseTimer pt(EWT_PHASE_QUERY, s);
-    mk<<<blocks, kQueryThreads, p.bytes, s>>>(
+    mk<<<blocks, threads, p.bytes, s>>>(
         t.view, types, static_cast<QueryRec<T> const*>(in), m,
         static_cast<uint64_t*>(out), t.err_d.as<uint32_t>(), p.stage_counts,
         p.stage_ranks);
@@ -325,15 +328,17 @@ void launch_typed(ewt_tree& t, uint8_t const* types, void const* in,
                                   static_cast<int>(kStageLimitBytes + 4096)));
     attr_set[ti][K] = true;
   }
+  uint32_t const threads = t.tune_threads[K] ? t.tune_threads[K] : kQueryThreads;
   int per_sm = 0;
   EWT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k,
-                                                         kQueryThreads, p.bytes));
+                                                         threads, p.bytes));
   per_sm = std::max(per_sm, 1);
-  uint64_t const need = ceil_div(m, kQueryThreads);
+  if (t.tune_blocks[K]) per_sm = std::min<int>(per_sm, t.tune_blocks[K]);
+  uint64_t const need = ceil_div(m, threads);
   uint64_t const full = uint64_t(per_sm) * sm_count();
   uint32_t const blocks = static_cast<uint32_t>(std::min(need, full));
   PhaseTimer pt(EWT_PHASE_QUERY, s);
-  k<<<blocks, kQueryThreads, p.bytes, s>>>(t.view, types, in, m, out,
+  k<<<blocks, threads, p.bytes, s>>>(t.view, types, in, m, out,
                                            t.err_d.as<uint32_t>(),
                                            p.stage_counts, p.stage_ranks);
   EWT_LAUNCHED();
@@ -406,6 +411,132 @@ void launch_mixed_raw(ewt_tree& t, uint8_t const* d_types, void const* d_q,
     case 2: launch_mixed_raw_typed<uint16_t>(t, d_types, d_q, m, d_out, d_err, s); break;
     case 4: launch_mixed_raw_typed<uint32_t>(t, d_types, d_q, m, d_out, d_err, s); break;
     default: launch_mixed_raw_typed<uint64_t>(t, d_types, d_q, m, d_out, d_err, s); break;
+  }
+}
+
+// ---- autotuner -------------------------------------------------------------
+namespace {
+
+__device__ __forceinline__ uint64_t probe_mix(uint64_t x) {  // splitmix64
+  x += 0x9e3779b97f4a7c15ull;
+  x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+  x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+  return x ^ (x >> 31);
+}
+
+// Valid probe queries over tree t: access i in [0, n); rank c uniform, i in
+// [0, n]; select c uniform, k in [1, count(c)] (k = 1 when c is absent);
+// kind 3 mixes them 40/40/20.
+template <class T>
+__global__ void __launch_bounds__(256)
+probe_kernel(TreeView t, int kind, uint64_t m, uint64_t seed,
+             uint8_t* __restrict__ types, QueryRec<T>* __restrict__ rec,
+             uint64_t* __restrict__ idx) {
+  uint64_t const stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < m;
+       i += stride) {
+    uint64_t const h = probe_mix(seed + i);
+    int ty = kind;
+    if (kind == 3) {
+      uint64_t const u = h % 5;
+      ty = u < 2 ? 0 : (u < 4 ? 1 : 2);
+    }
+    uint64_t const h2 = probe_mix(h);
+    uint64_t const c = h2 % t.sigma;
+    uint64_t index;
+    if (ty == 0) {
+      index = h2 % t.n;
+    } else if (ty == 1) {
+      index = probe_mix(h2) % (t.n + 1);
+    } else {
+      uint64_t const cnt = (c + 1 < t.sigma ? t.counts[c + 1] : t.n) - t.counts[c];
+      index = cnt ? 1 + probe_mix(h2) % cnt : 1;
+    }
+    T const sym = t.is_min ? static_cast<T>(c)
+                           : static_cast<T const*>(t.alphabet)[c];
+    if (kind == 0) {
+      idx[i] = index;
+    } else {
+      rec[i].index = index;
+      rec[i].symbol = sym;
+      if (kind == 3) types[i] = static_cast<uint8_t>(ty);
+    }
+  }
+}
+
+template <class T>
+void autotune_typed(ewt_tree& t, uint64_t m, ewt_tuning* out) {
+  cudaStream_t const s = t.stream;
+  DevBuf types(m), rec(m * 16), idx(m * 8), res(m * 8);
+  uint32_t const sms = static_cast<uint32_t>(sm_count());
+  cudaEvent_t e0, e1;
+  EWT_CUDA(cudaEventCreate(&e0));
+  EWT_CUDA(cudaEventCreate(&e1));
+  uint32_t const thread_opts[2] = {128, 256};
+  uint32_t const block_opts[5] = {0, 2, 4, 6, 8};  // 0: as many as fit
+  for (int kind = 0; kind < 4; ++kind) {
+    probe_kernel<T><<<std::min<uint64_t>(ceil_div(m, 256), uint64_t(sms) * 8), 256, 0, s>>>(
+        t.view, kind, m, 0x5eed0000ull + kind, types.as<uint8_t>(),
+        rec.as<QueryRec<T>>(), idx.as<uint64_t>());
+    EWT_LAUNCHED();
+    auto run = [&]() {
+      switch (kind) {
+        case 0: launch_typed<T, kAccess>(t, nullptr, idx.get(), m, res.get(), s); break;
+        case 1: launch_typed<T, kRank>(t, nullptr, rec.get(), m, res.get(), s); break;
+        case 2: launch_typed<T, kSelect>(t, nullptr, rec.get(), m, res.get(), s); break;
+        default: launch_typed<T, kMixed>(t, types.as<uint8_t>(), rec.get(), m, res.get(), s); break;
+      }
+    };
+    auto timed = [&]() -> float {
+      run();  // warm
+      EWT_CUDA(cudaEventRecord(e0, s));
+      for (int r = 0; r < 3; ++r) run();
+      EWT_CUDA(cudaEventRecord(e1, s));
+      EWT_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      EWT_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      return ms / 3;
+    };
+    t.tune_threads[kind] = 0;
+    t.tune_blocks[kind] = 0;
+    float const base = timed();
+    float best = base;
+    uint32_t bt = 0, bb = 0;
+    for (uint32_t th : thread_opts)
+      for (uint32_t bl : block_opts) {
+        t.tune_threads[kind] = th;
+        t.tune_blocks[kind] = bl;
+        float const ms = timed();
+        if (ms < best) {
+          best = ms;
+          bt = th;
+          bb = bl;
+        }
+      }
+    t.tune_threads[kind] = bt;
+    t.tune_blocks[kind] = bb;
+    if (out) {
+      out->threads[kind] = bt ? bt : kQueryThreads;
+      out->blocks_per_sm[kind] = bb;
+      out->default_mq_s[kind] = m / (base * 1e3);
+      out->tuned_mq_s[kind] = m / (best * 1e3);
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  // the probes are valid queries; clear the invalid-query word regardless
+  EWT_CUDA(cudaMemsetAsync(t.err_d.get(), 0, 4, s));
+  EWT_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace
+
+void autotune_queries(ewt_tree& t, uint64_t probe_queries, ewt_tuning* out) {
+  switch (t.elem_size) {
+    case 1: autotune_typed<uint8_t>(t, probe_queries, out); break;
+    case 2: autotune_typed<uint16_t>(t, probe_queries, out); break;
+    case 4: autotune_typed<uint32_t>(t, probe_queries, out); break;
+    default: autotune_typed<uint64_t>(t, probe_queries, out); break;
   }
 }
 

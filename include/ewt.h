@@ -215,6 +215,21 @@ int ewt_abi_version(void);
 /* Number of kernel launches this library issued since load (all threads). */
 uint64_t ewt_launch_count(void);
 
+/* ---- autotuning -----------------------------------------------------------
+ * Times the query kernels of every kind (access, rank, select, mixed) on
+ * probe_queries device-generated valid queries over this tree for candidate
+ * launch shapes (threads per CTA x resident CTAs per SM) and keeps the
+ * fastest per kind for every later launch on this tree; *out (may be NULL)
+ * reports the choice and the default and tuned rates.  Results never
+ * depend on the launch shape.  No reference counterpart (the reference's
+ * launch configuration is fixed per call site, utils.cu:42-94). */
+typedef struct ewt_tuning {
+  uint32_t threads[4];       /* threads per CTA: access, rank, select, mixed */
+  uint32_t blocks_per_sm[4]; /* resident CTAs per SM; 0 = as many as fit    */
+  double default_mq_s[4], tuned_mq_s[4];
+} ewt_tuning;
+int ewt_autotune(ewt_tree* tree, uint64_t probe_queries, ewt_tuning* out);
+
 /* ---- index files --------------------------------------------------------
  * Writes a built tree (shape, level bits, RankSelect counts and samples,
  * rank blocks, count table, node ranks) to `path`; ewt_load reads it back

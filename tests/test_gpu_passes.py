@@ -139,3 +139,26 @@ def test_detected_wide_alphabet(ewt, oracle, dtype, sigma):
     assert np.array_equal(gt.getAlphabet(), np.sort(vals))
     assert_same_tree(gt, ot)
     check_queries(gt, ot, text, np.sort(vals).astype(np.uint64), 3_000, seed=6)
+
+
+@pytest.mark.parametrize("dtype,sigma,minimal", [(np.uint8, 256, True),
+                                                 (np.uint16, 3000, False),
+                                                 (np.uint32, 77, False)])
+def test_autotuned_queries_exact(ewt, oracle, dtype, sigma, minimal):
+    """After ewt_autotune picked a launch shape per query kind, every kind
+    still answers exactly as the plain scan (the shape changes speed only)."""
+    from tests.workloads import random_text
+    rng = np.random.default_rng(sigma + 1)
+    text, alphabet = random_text(rng, 300_000, sigma, dtype, minimal=minimal)
+    gt = ewt.WaveletTree(text, alphabet)
+    tuning = gt.autotune(1 << 14)
+    assert set(tuning) == {"access", "rank", "select", "mixed"}
+    for kind, r in tuning.items():
+        assert r["threads"] in (128, 256), (kind, r)
+        assert r["blocks_per_sm"] in (0, 2, 4, 6, 8), (kind, r)
+        assert r["tuned_mq_s"] >= r["default_mq_s"] > 0, (kind, r)
+    ot = oracle.OracleTree(text, alphabet)
+    al = np.asarray(alphabet, dtype=np.uint64)
+    check_queries(gt, ot, text, al, 20_000, seed=9)
+    with pytest.raises(ewt.EwtError):
+        gt.autotune(10)  # below the probe minimum
