@@ -9,6 +9,10 @@ timed steps the same tree answers 2^26 mixed queries (40 % access, 40 %
 rank, 20 % select, types interleaved at random) in the batched one-launch
 form and in the plain per-type form, device-resident and end to end from
 pinned host memory; the sweep over sigma in {4, 16, 64} is timed once each.
+Further sections: 256 uneven texts built and queried together, the serving
+loop under Poisson load, the standalone RankSelect, and uint16 texts of
+3 * 2^30 symbols over sigma 65536 (Zipf 1.1) and 1024 with autotuned and
+graph-replayed query launches.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -54,9 +58,12 @@ def parse():
                    help="skip the serving-loop rate sweep")
     p.add_argument("--no-rs", action="store_true",
                    help="skip the standalone RankSelect comparison")
+    p.add_argument("--no-large", action="store_true",
+                   help="skip the uint16 large-alphabet build and queries")
     p.add_argument("--cpu-sample", type=int, default=1 << 25)
     p.add_argument("--only", default="all",
-                   choices=["all", "build", "queries", "multi", "serve", "rs"],
+                   choices=["all", "build", "queries", "multi", "serve", "rs",
+                            "large"],
                    help="build: stop after the timed builds; queries: also "
                         "time the query batches (for profiling runs)")
     return p.parse_args()
@@ -433,6 +440,127 @@ def bench_rank_select(torch, E, dev, seed=11):
             "select_gpu_over_cpu": (m / sel_s) / (mc / cpu_sel_s)}
 
 
+def bench_large_alphabet(torch, E, dev, gen, n=3 * GIB, m=1 << 26):
+    """Uint16 texts of 3*2^30 symbols (device-resident): sigma = 65536 with
+    Zipf(1.1) symbols and sigma = 1024 uniform.  Each is built once timed,
+    then answers 2^26 mixed queries (40/40/20, types interleaved) as plain
+    per-type launches, as one batched launch, both again after the library
+    autotuned the launch shapes, and as a CUDA graph replay of the tuned
+    batched launch."""
+    import ctypes
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    L = E.lib()
+    res = {}
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    for sigma, zipf in ((65536, 1.1), (1024, None)):
+        text = torch.empty(n, dtype=torch.int16, device=dev)
+        chunk = 1 << 27
+        if zipf is None:
+            for a in range(0, n, chunk):
+                b = min(n, a + chunk)
+                text[a:b] = torch.randint(0, sigma, (b - a,), device=dev,
+                                          generator=gen).to(torch.int16)
+        else:
+            w = 1.0 / torch.arange(1, sigma + 1, device=dev,
+                                   dtype=torch.float64) ** zipf
+            cdf = torch.cumsum(w, 0) / w.sum()
+            for a in range(0, n, chunk):
+                b = min(n, a + chunk)
+                u = torch.rand(b - a, device=dev, dtype=torch.float64,
+                               generator=gen)
+                ids = torch.searchsorted(cdf, u).clamp_(max=sigma - 1)
+                text[a:b] = ids.to(torch.int32).to(torch.int16)  # low 16 bits
+            del w, cdf, u, ids
+        alph = np.arange(sigma, dtype=np.uint16)
+
+        def build():
+            h = ctypes.c_void_p()
+            st = L.ewt_build(text.data_ptr(), n, 2, alph.ctypes.data, sigma, 0,
+                             ctypes.byref(h))
+            assert st == 0, st
+            return E.WaveletTree(None, _handle=h.value)
+
+        build().close()
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        tree = build()
+        torch.cuda.synchronize()
+        build_s = time.perf_counter() - a
+        types, rec = make_mixed_queries(torch, tree, n, sigma, m, gen)
+        out = torch.empty(m, dtype=torch.int64, device=dev)
+        sel = {t: torch.nonzero(types == t).squeeze(1) for t in (0, 1, 2)}
+        acc_idx = rec[sel[0], 0].contiguous()
+        rq = rec[sel[1]].contiguous()
+        sq = rec[sel[2]].contiguous()
+        o_acc = torch.empty(acc_idx.numel(), dtype=torch.int16, device=dev)
+        o_r = torch.empty(rq.shape[0], dtype=torch.int64, device=dev)
+        o_s = torch.empty(sq.shape[0], dtype=torch.int64, device=dev)
+
+        def mixed():
+            tree.mixed_device(types.data_ptr(), rec.data_ptr(), m,
+                              out.data_ptr(), sptr)
+
+        def plain():
+            return (timed(lambda: tree.access_device(
+                        acc_idx.data_ptr(), acc_idx.numel(), o_acc.data_ptr(), sptr))
+                    + timed(lambda: tree.rank_device(
+                        rq.data_ptr(), rq.shape[0], o_r.data_ptr(), sptr))
+                    + timed(lambda: tree.select_device(
+                        sq.data_ptr(), sq.shape[0], o_s.data_ptr(), sptr)))
+
+        mixed_ms = timed(mixed)
+        plain_ms = plain()
+        assert tree.query_status(sptr) == 0
+        want = out.clone()
+        tuning = tree.autotune(1 << 22)
+        tuned_mixed_ms = timed(mixed)
+        tuned_plain_ms = plain()
+        assert tree.query_status(sptr) == 0
+        assert torch.equal(out, want)  # the launch shape changes no answer
+        # the tuned batched launch captured once, replayed
+        side = torch.cuda.Stream()
+        side.wait_stream(stream)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=side):
+            tree.mixed_device(types.data_ptr(), rec.data_ptr(), m,
+                              out.data_ptr(), side.cuda_stream)
+        out.zero_()
+        graph_ms = timed(graph.replay)
+        assert tree.query_status(sptr) == 0
+        assert torch.equal(out, want)
+        key = "sigma%d_%s" % (sigma, "zipf1.1" if zipf else "uniform")
+        res[key] = {
+            "n": n, "sigma": sigma, "levels": int(tree.info.levels),
+            "build_GB_s": 2 * n / build_s / 1e9, "build_ms": build_s * 1e3,
+            "queries": m,
+            "batched_mixed_Mq_s": m / mixed_ms / 1e3,
+            "plain_per_type_Mq_s": m / plain_ms / 1e3,
+            "autotuned": {"shapes": {k: [v["threads"], v["blocks_per_sm"]]
+                                     for k, v in tuning.items()},
+                          "batched_mixed_Mq_s": m / tuned_mixed_ms / 1e3,
+                          "plain_per_type_Mq_s": m / tuned_plain_ms / 1e3,
+                          "graph_replay_mixed_Mq_s": m / graph_ms / 1e3},
+        }
+        del graph, out, want, types, rec, acc_idx, rq, sq, o_acc, o_r, o_s, sel
+        tree.close()
+        del text
+        torch.cuda.empty_cache()
+    return res
+
+
 def make_mixed_queries(torch, tree, n, sigma, m, gen):
     """Device-resident mixed batch: types 40/40/20, RankSelectQuery records."""
     dev = "cuda"
@@ -473,11 +601,14 @@ def run_ours(args, world, rank, local):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    if args.only in ("multi", "serve", "rs"):
+    if args.only in ("multi", "serve", "rs", "large"):
         if args.only == "multi":
             key, part = "many_texts", bench_multi_text(torch, E, dev, gen)
         elif args.only == "serve":
             key, part = "serving", bench_serving(torch, E, dev, gen, text)
+        elif args.only == "large":
+            del text
+            key, part = "large_alphabet_u16", bench_large_alphabet(torch, E, dev, gen)
         else:
             key, part = "rank_select", bench_rank_select(torch, E, dev)
         if rank == 0:
@@ -695,6 +826,11 @@ def run_ours(args, world, rank, local):
     rsel = None
     if not args.no_rs and rank == 0 and world == 1:
         rsel = bench_rank_select(torch, E, dev)
+    large = None
+    if not args.no_large:
+        del text
+        torch.cuda.empty_cache()
+        large = bench_large_alphabet(torch, E, dev, gen)
 
     # ---- CPU baseline (rank 0, N = 1 only) ---------------------------------
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -735,6 +871,7 @@ def run_ours(args, world, rank, local):
             "roofline": roofline, "build": build, "queries": queries,
             "sigma_sweep_GB_s": sweep, "e2e": e2e, "cpu_baseline": cpu,
             "many_texts": multi, "serving": serve, "rank_select": rsel,
+            "large_alphabet_u16": large,
             "clocks": clk,
         }
         print(json.dumps(line))

@@ -215,6 +215,21 @@ inline int sm_count() {
 
 inline uint64_t ceil_div(uint64_t a, uint64_t b) { return (a + b - 1) / b; }
 
+// Puts this thread's stream-capture mode to relaxed for its scope, so that
+// the host-side launch preparation (kernel attributes, occupancy queries) of
+// a launch made while the caller captures a CUDA graph is permitted in every
+// capture mode; restores the caller's mode on exit.
+class RelaxedCapture {
+ public:
+  RelaxedCapture() { cudaThreadExchangeStreamCaptureMode(&mode_); }
+  ~RelaxedCapture() { cudaThreadExchangeStreamCaptureMode(&mode_); }
+  RelaxedCapture(RelaxedCapture const&) = delete;
+  RelaxedCapture& operator=(RelaxedCapture const&) = delete;
+
+ private:
+  cudaStreamCaptureMode mode_ = cudaStreamCaptureModeRelaxed;
+};
+
 // Event-timed phase on one stream (ewt_set_timing / ewt_get_timing).  When
 // timing is off the guard does nothing.
 bool timing_enabled();
@@ -224,6 +239,12 @@ class PhaseTimer {
  public:
   PhaseTimer(int phase, cudaStream_t s) : phase_(phase), s_(s) {
     if (!timing_enabled()) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s_, &cs) != cudaSuccess ||
+        cs != cudaStreamCaptureStatusNone) {  // a graph is being captured
+      (void)cudaGetLastError();
+      return;
+    }
     if (cudaEventCreate(&a_) != cudaSuccess || cudaEventCreate(&b_) != cudaSuccess) {
       (void)cudaGetLastError();
       return;

@@ -293,6 +293,7 @@ void launch_typed(ewt_tree& t, uint8_t const* types, void const* in,
               EWT_ERR_INVALID_ARGUMENT,
               "query and result buffers must be 8-byte aligned");
   StagePlan const p = plan_stage(t);
+  RelaxedCapture relaxed;  // these launches may be captured into a graph
   if (K == kMixed) {
     auto mk = mixed_kernel<T>;
     static thread_local bool mattr[4] = {};
