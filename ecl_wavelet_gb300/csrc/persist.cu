@@ -2,7 +2,7 @@
 // rebuilding (ewt_save / ewt_load).  The reference has no serialisation; a
 // serving process uses this to admit prebuilt indexes.
 //
-// Layout (little-endian): the magic "EWTIDX01", a header of 64-bit fields,
+// Layout (little-endian): the magic "EWTIDX02", a header of 64-bit fields,
 // the host-side shape (alphabet, count table, codes, node starts, nodes per
 // level, node bases, level sizes, per-array metadata), then the device arrays
 // in a fixed order (level words, L1, L2, samples of zeros and ones, rank
@@ -19,7 +19,7 @@
 namespace ewt {
 namespace {
 
-constexpr char kMagic[8] = {'E', 'W', 'T', 'I', 'D', 'X', '0', '1'};
+constexpr char kMagic[8] = {'E', 'W', 'T', 'I', 'D', 'X', '0', '2'};
 constexpr size_t kPiece = size_t(64) << 20;
 
 struct File {

@@ -81,6 +81,11 @@ RSView RSStore::view() const {
   v.s1 = s1.as<uint64_t>();
   v.meta = meta_d.as<ArrayMeta>();
   v.rb = rb.get() ? rb.as<uint4>() : nullptr;
+  if (v.rb && !meta.empty()) {  // the high-count table follows the blocks
+    uint64_t const blocks =
+        meta.back().rb_off + ceil_div(meta.back().bits, ecl::detail::kRankBlockBits);
+    v.rbh = reinterpret_cast<uint64_t const*>(rb.as<unsigned char>() + blocks * 32);
+  }
   v.num_arrays = static_cast<uint32_t>(meta.size());
   return v;
 }
@@ -317,12 +322,15 @@ void build_rs_samples(RSStore& rs, cudaStream_t stream) {
 
 namespace {
 
-// One thread per rank block (64-byte line) of every array: the number of
-// ones before the block (from the L1/L2 counts) and the block's 14 words.
+// One thread per rank block (32-byte sector) of every array: the low word
+// of the ones before the block (from the L1/L2 counts) and the block's 7
+// words; the first block of every 2^24 also writes the full count to the
+// high-count table.
 __global__ void __launch_bounds__(256)
 rank_blocks_kernel(RSView v, uint64_t const* __restrict__ line_start,
                    uint32_t num_arrays, uint64_t total_lines,
-                   uint64_t total_words, uint4* __restrict__ out) {
+                   uint64_t total_words, uint4* __restrict__ out,
+                   uint64_t* __restrict__ high) {
   uint64_t const g = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   if (g >= total_lines) return;
   uint32_t lo = 0, hi = num_arrays - 1;
@@ -339,12 +347,11 @@ rank_blocks_kernel(RSView v, uint64_t const* __restrict__ line_start,
 #pragma unroll
   for (uint32_t j = 0; j < ecl::detail::kRankBlockWords; ++j)
     w[j] = w0 + j < total_words ? v.words[w0 + j] : 0u;
-  uint4* line = out + g * 4;
-  line[0] = make_uint4(static_cast<uint32_t>(ones),
-                       static_cast<uint32_t>(ones >> 32), w[0], w[1]);
-  line[1] = make_uint4(w[2], w[3], w[4], w[5]);
-  line[2] = make_uint4(w[6], w[7], w[8], w[9]);
-  line[3] = make_uint4(w[10], w[11], w[12], w[13]);
+  uint4* line = out + g * 2;
+  line[0] = make_uint4(static_cast<uint32_t>(ones), w[0], w[1], w[2]);
+  line[1] = make_uint4(w[3], w[4], w[5], w[6]);
+  if ((b & ((uint64_t(1) << ecl::detail::kRankHighShift) - 1)) == 0)
+    high[m.rbh_off + (b >> ecl::detail::kRankHighShift)] = ones;
 }
 
 }  // namespace
@@ -352,13 +359,18 @@ rank_blocks_kernel(RSView v, uint64_t const* __restrict__ line_start,
 void build_rank_blocks(RSStore& rs, cudaStream_t stream) {
   uint32_t const count = static_cast<uint32_t>(rs.meta.size());
   std::vector<uint64_t> start(count);
-  uint64_t total = 0;
+  uint64_t total = 0, highs = 0;
   for (uint32_t a = 0; a < count; ++a) {
     rs.meta[a].rb_off = total;
+    rs.meta[a].rbh_off = highs;
     start[a] = total;
-    total += ceil_div(rs.meta[a].bits, ecl::detail::kRankBlockBits);
+    uint64_t const blocks = ceil_div(rs.meta[a].bits, ecl::detail::kRankBlockBits);
+    total += blocks;
+    highs += ceil_div(std::max<uint64_t>(blocks, 1),
+                      uint64_t(1) << ecl::detail::kRankHighShift);
   }
-  rs.rb.alloc(total * 64);
+  // blocks, then the high-count table in the same allocation
+  rs.rb.alloc(total * 32 + highs * 8);
   DevBuf start_d(count * 8);
   EWT_CUDA(cudaMemcpyAsync(start_d.get(), start.data(), count * 8,
                            cudaMemcpyHostToDevice, stream));
@@ -371,7 +383,9 @@ void build_rank_blocks(RSStore& rs, cudaStream_t stream) {
     PhaseTimer pt(EWT_PHASE_SAMPLES, stream);
     rank_blocks_kernel<<<static_cast<uint32_t>(ceil_div(total, 256)), 256, 0,
                          stream>>>(v, start_d.as<uint64_t>(), count, total,
-                                   rs.total_words, rs.rb.as<uint4>());
+                                   rs.total_words, rs.rb.as<uint4>(),
+                                   reinterpret_cast<uint64_t*>(
+                                       rs.rb.as<unsigned char>() + total * 32));
     EWT_LAUNCHED();
   }
   EWT_CUDA(cudaStreamSynchronize(stream));

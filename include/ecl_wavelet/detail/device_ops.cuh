@@ -43,15 +43,21 @@ struct ArrayMeta {
   uint64_t ones;        // total number of ones
   uint64_t num_l1;      // number of L1 blocks
   uint64_t num_last_l2; // L2 blocks inside the last L1 block
-  uint64_t rb_off;      // first rank block (64-byte line) of the array
+  uint64_t rb_off;      // first rank block (32-byte sector) of the array
+  uint64_t rbh_off;     // first high-count entry of the array
 };
 
-/* Query-side rank blocks: each 64-byte line holds the number of ones before
- * its first bit (uint64) followed by 448 bits of the array, so a rank reads
- * one line.  An auxiliary copy next to the reference-format arrays, which
- * stay the source of truth for exports and select. */
-constexpr uint64_t kRankBlockBits = 448;
+/* Query-side rank blocks: each 32-byte block (one DRAM sector) holds the low
+ * 32 bits of the number of ones before its first bit followed by 224 bits of
+ * the array, so a rank reads one sector.  The high part comes from a small
+ * table with the full count before every 2^24-th block (within 2^24 blocks
+ * the count grows by less than 2^32, so the low word fixes it; arrays shorter
+ * than 2^24 blocks never read the table).  An auxiliary copy next to the
+ * reference-format arrays, which stay the source of truth for exports and
+ * select. */
+constexpr uint64_t kRankBlockBits = 224;
 constexpr uint64_t kRankBlockWords = kRankBlockBits / 32;
+constexpr uint32_t kRankHighShift = 24;
 
 /* A set of bit arrays with rank/select support, all in device memory. */
 struct RSView {
@@ -61,7 +67,8 @@ struct RSView {
   const uint64_t* s0;
   const uint64_t* s1;
   const ArrayMeta* meta;  // device array of num_arrays entries
-  const uint4* rb;        // rank blocks (4 uint4 per line), may be null
+  const uint4* rb;        // rank blocks (2 uint4 per block), may be null
+  const uint64_t* rbh;    // high counts of the rank blocks
   uint32_t num_arrays;
   uint32_t reserved;
 };
@@ -135,21 +142,15 @@ __device__ __forceinline__ uint64_t rs_rank1(const RSView& v,
     return m.ones;
   }
   if (v.rb) {
-    // One 64-byte line: ones before the block + 14 data words.
+    // One 32-byte block: low word of the ones before it + 7 data words.
     uint64_t const blk = pos / kRankBlockBits;
     uint32_t const off = static_cast<uint32_t>(pos - blk * kRankBlockBits);
-    uint4 const* line = v.rb + (m.rb_off + blk) * 4;
+    uint4 const* line = v.rb + (m.rb_off + blk) * 2;
     uint32_t const wi = off >> 5;
     uint4 const q0 = __ldg(line);
     uint4 const q1 = __ldg(line + 1);
-    uint4 q2 = make_uint4(0, 0, 0, 0), q3 = q2;
-    if (wi >= 6) {
-      q2 = __ldg(line + 2);
-      q3 = __ldg(line + 3);
-    }
-    uint32_t const w[kRankBlockWords] = {q0.z, q0.w, q1.x, q1.y, q1.z,
-                                         q1.w, q2.x, q2.y, q2.z, q2.w,
-                                         q3.x, q3.y, q3.z, q3.w};
+    uint32_t const w[kRankBlockWords] = {q0.y, q0.z, q0.w, q1.x,
+                                         q1.y, q1.z, q1.w};
     uint32_t acc = 0, cur = 0;
 #pragma unroll
     for (uint32_t j = 0; j < kRankBlockWords; ++j) {
@@ -158,7 +159,13 @@ __device__ __forceinline__ uint64_t rs_rank1(const RSView& v,
     }
     acc += __popc(cur & ((1u << (off & 31)) - 1u));
     if (GetBit) *bit = (cur >> (off & 31)) & 1u;
-    return ((uint64_t(q0.y) << 32) | q0.x) + acc;
+    uint64_t before = q0.x;
+    uint64_t const hj = blk >> kRankHighShift;
+    if (hj) {
+      uint64_t const h = __ldg(v.rbh + m.rbh_off + hj);
+      before = h + static_cast<uint32_t>(q0.x - static_cast<uint32_t>(h));
+    }
+    return before + acc;
   }
   uint64_t const b2 = pos >> 9;
   uint64_t r = __ldg(v.l1 + m.l1_off + (pos >> 16));

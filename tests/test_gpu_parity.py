@@ -279,34 +279,41 @@ def test_device_resident_batches(ewt, oracle):
                           ot.scan_rank(rk, rs)[0])
 
 
-def test_large_text_round_trips(ewt):
-    """n > 2^31 exercises 64-bit positions; size-independent properties."""
+@pytest.mark.parametrize("n,sigma", [((1 << 31) + 12345, 256),
+                                     ((1 << 32) + 777, 4)])
+def test_large_text_round_trips(ewt, n, sigma):
+    """n > 2^31 exercises 64-bit positions, n > 2^32 also level arrays
+    longer than 2^24 rank blocks (their counts need the high-count table);
+    size-independent properties: rank answers (rank blocks) agree with
+    select answers (L1/L2 counts and samples) and with the text itself."""
     torch = pytest.importorskip("torch")
-    n = (1 << 31) + 12345
     g = torch.Generator(device="cuda").manual_seed(3)
-    dtext = torch.randint(0, 256, (n,), dtype=torch.uint8, device="cuda",
+    dtext = torch.randint(0, sigma, (n,), dtype=torch.uint8, device="cuda",
                           generator=g)
-    t = ewt.WaveletTree(dtext, np.arange(256))
+    t = ewt.WaveletTree(dtext, np.arange(sigma))
     counts = t.export("COUNTS").astype(np.int64)
     occ = np.diff(np.append(counts, n))
-    hist = torch.bincount(dtext.to(torch.int32), minlength=256).cpu().numpy()
+    hist = torch.bincount(dtext.to(torch.int32), minlength=sigma).cpu().numpy()
     assert np.array_equal(occ, hist)
-    # level 0 holds bit 7 of every symbol in text order
+    # level 0 holds the top code bit of every symbol in text order
     w0 = t.export("LEVEL_WORDS", 0)
-    assert int(np.unpackbits(w0.view(np.uint8)).sum()) == int(hist[128:].sum())
+    assert int(np.unpackbits(w0.view(np.uint8)).sum()) == int(hist[sigma // 2:].sum())
     rng = np.random.default_rng(4)
     m = 200_000
-    sym = rng.integers(0, 256, m).astype(np.uint64)
+    sym = rng.integers(0, sigma, m).astype(np.uint64)
     k = (rng.random(m) * occ[sym]).astype(np.uint64) + 1
     pos = t.select(t.make_queries(k, sym))
     assert (pos < n).all()
     assert np.array_equal(t.access(pos).astype(np.uint64), sym)
     assert np.array_equal(t.rank(t.make_queries(pos, sym)), k - 1)
     idx = rng.integers(0, n, m).astype(np.uint64)
+    edge = 224 << 24  # first bit covered by the second high-count entry
+    near = np.arange(edge - 300, edge + 300, dtype=np.uint64)
+    idx = np.concatenate([idx, near[near < n]])
     c = t.access(idx).astype(np.uint64)
     assert np.array_equal(c, dtext[torch.from_numpy(idx.view(np.int64)).cuda()]
                           .cpu().numpy())
     r = t.rank(t.make_queries(idx, c))
     assert np.array_equal(t.select(t.make_queries(r + 1, c)), idx)
-    assert np.array_equal(t.rank(t.make_queries(np.full(256, n), np.arange(256))),
+    assert np.array_equal(t.rank(t.make_queries(np.full(sigma, n), np.arange(sigma))),
                           occ.astype(np.uint64))
