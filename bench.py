@@ -39,6 +39,7 @@ sys.path.insert(0, REPO)
 METRIC = ("Mqueries/s (access/rank/select) + build GB/s; batched vs plain, "
           "bit-exact")
 GIB = 1 << 30
+KINDS = ("access", "rank", "select", "mixed")
 
 
 def parse():
@@ -549,7 +550,8 @@ def bench_large_alphabet(torch, E, dev, gen, n=3 * GIB, m=1 << 26):
             "batched_mixed_Mq_s": m / mixed_ms / 1e3,
             "plain_per_type_Mq_s": m / plain_ms / 1e3,
             "autotuned": {"shapes": {k: [v["threads"], v["blocks_per_sm"]]
-                                     for k, v in tuning.items()},
+                                     for k, v in tuning.items() if k in KINDS},
+                          "select_sample_rate": tuning["select_sample_rate"],
                           "batched_mixed_Mq_s": m / tuned_mixed_ms / 1e3,
                           "plain_per_type_Mq_s": m / tuned_plain_ms / 1e3,
                           "graph_replay_mixed_Mq_s": m / graph_ms / 1e3},
@@ -758,7 +760,8 @@ def run_ours(args, world, rank, local):
     assert tree.query_status(sptr) == 0
     queries = {
         "autotuned": {"shapes": {k: [v["threads"], v["blocks_per_sm"]]
-                                 for k, v in tuning.items()},
+                                 for k, v in tuning.items() if k in KINDS},
+                      "select_sample_rate": tuning["select_sample_rate"],
                       "batched_mixed_Mq_s": m / tuned_mixed_ms / 1e3,
                       "plain_per_type_Mq_s": m / tuned_plain_ms / 1e3},
         "n_queries": m, "mix": "40/40/20 access/rank/select, interleaved",

@@ -71,6 +71,7 @@ class Tuning(C.Structure):
     """Launch shapes chosen by ewt_autotune per query kind (access, rank,
     select, mixed) and the probe rates they gave."""
     _fields_ = [("threads", C.c_uint32 * 4), ("blocks_per_sm", C.c_uint32 * 4),
+                ("select_sample_rate", C.c_uint32), ("reserved", C.c_uint32),
                 ("default_mq_s", C.c_double * 4), ("tuned_mq_s", C.c_double * 4)]
 
 
@@ -133,6 +134,8 @@ SIGNATURES = {
                                          C.c_void_p, C.c_void_p, C.c_uint64,
                                          C.c_void_p, C.c_void_p, C.c_void_p]),
     "ewt_autotune": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Tuning)]),
+    "ewt_set_select_samples": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "ewt_rs_set_select_samples": (C.c_int, [C.c_void_p, C.c_uint32]),
     "ewt_launch_count": (C.c_uint64, []),
     "ewt_set_timing": (None, [C.c_int]),
     "ewt_get_timing": (None, [C.c_void_p, C.c_int]),
@@ -318,17 +321,26 @@ class WaveletTree:
 
     def autotune(self, probe_queries: int = 1 << 22) -> dict:
         """Times the query kernels on `probe_queries` device-generated valid
-        queries per kind for candidate launch shapes and keeps the fastest
-        for every later query on this tree (ewt_autotune).  Returns, per
-        kind, the chosen threads per CTA, resident CTAs per SM (0 = as many
-        as fit) and the default and tuned rates in million queries/s."""
+        queries for candidate dense select-sample rates and, per kind, launch
+        shapes, and keeps the fastest for every later query on this tree
+        (ewt_autotune).  Returns, per kind, the chosen threads per CTA,
+        resident CTAs per SM (0 = as many as fit) and the default and tuned
+        rates in million queries/s, and under "select_sample_rate" the dense
+        sample rate kept (0: reference-format samples only)."""
         tu = Tuning()
         _check(lib().ewt_autotune(self._h, probe_queries, C.byref(tu)), "autotune")
-        return {kind: {"threads": tu.threads[i],
-                       "blocks_per_sm": tu.blocks_per_sm[i],
-                       "default_mq_s": tu.default_mq_s[i],
-                       "tuned_mq_s": tu.tuned_mq_s[i]}
-                for i, kind in enumerate(("access", "rank", "select", "mixed"))}
+        res = {kind: {"threads": tu.threads[i],
+                      "blocks_per_sm": tu.blocks_per_sm[i],
+                      "default_mq_s": tu.default_mq_s[i],
+                      "tuned_mq_s": tu.tuned_mq_s[i]}
+               for i, kind in enumerate(("access", "rank", "select", "mixed"))}
+        res["select_sample_rate"] = tu.select_sample_rate
+        return res
+
+    def set_select_samples(self, rate: int):
+        """Dense select samples every `rate` zeros / ones (0: none; a power
+        of two in [32, 65536]) (ewt_set_select_samples)."""
+        _check(lib().ewt_set_select_samples(self._h, rate), "set_select_samples")
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
@@ -462,6 +474,10 @@ class RankSelect:
                                   bits.size, gpu_index, C.byref(self._h)),
                "RankSelect")
         self.bits = bits
+
+    def set_select_samples(self, rate: int):
+        """As WaveletTree.set_select_samples (ewt_rs_set_select_samples)."""
+        _check(lib().ewt_rs_set_select_samples(self._h, rate), "set_select_samples")
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

@@ -544,6 +544,7 @@ int ewt_get_device_view(const ewt_tree* t, void* view_out, uint64_t view_size) {
     EWT_REQUIRE(t && view_out, EWT_ERR_INVALID_ARGUMENT, "null argument");
     EWT_REQUIRE(view_size == sizeof(TreeView), EWT_ERR_INVALID_ARGUMENT,
                 "view size does not match this library's TreeView");
+    t->view_shared.store(true);
     std::memcpy(view_out, &t->view, sizeof(TreeView));
   });
 }
@@ -656,8 +657,50 @@ int ewt_rs_get_device_view(const ewt_rs* r, void* view_out, uint64_t view_size) 
     EWT_REQUIRE(r && view_out, EWT_ERR_INVALID_ARGUMENT, "null argument");
     EWT_REQUIRE(view_size == sizeof(RSView), EWT_ERR_INVALID_ARGUMENT,
                 "view size does not match this library's RSView");
+    r->view_shared.store(true);
     RSView const v = r->rs.view();
     std::memcpy(view_out, &v, sizeof(RSView));
+  });
+}
+
+namespace {
+uint32_t sample_shift(uint32_t rate) {
+  EWT_REQUIRE(rate == 0 || (rate >= 32 && rate <= 65536 && (rate & (rate - 1)) == 0),
+              EWT_ERR_INVALID_ARGUMENT,
+              "select sample rate must be 0 or a power of two in [32, 65536]");
+  uint32_t sh = 0;
+  while (rate > 1) {
+    rate >>= 1;
+    ++sh;
+  }
+  return sh;
+}
+}  // namespace
+
+int ewt_set_select_samples(ewt_tree* t, uint32_t rate) {
+  return guarded([&] {
+    EWT_REQUIRE(t != nullptr, EWT_ERR_INVALID_ARGUMENT, "tree is null");
+    uint32_t const sh = sample_shift(rate);
+    std::lock_guard<std::mutex> lk(t->query_mu);
+    EWT_REQUIRE(!t->view_shared.load(), EWT_ERR_INVALID_ARGUMENT,
+                "the tree's device view was copied out; its samples stay");
+    DeviceGuard g(t->device);
+    AllocStream as(t->stream);
+    build_dense_samples(t->rs, sh, t->stream);
+    t->view.rs = t->rs.view();
+  });
+}
+
+int ewt_rs_set_select_samples(ewt_rs* r, uint32_t rate) {
+  return guarded([&] {
+    EWT_REQUIRE(r != nullptr, EWT_ERR_INVALID_ARGUMENT, "rank/select is null");
+    uint32_t const sh = sample_shift(rate);
+    std::lock_guard<std::mutex> lk(r->query_mu);
+    EWT_REQUIRE(!r->view_shared.load(), EWT_ERR_INVALID_ARGUMENT,
+                "the device view was copied out; its samples stay");
+    DeviceGuard g(r->device);
+    AllocStream as(r->stream);
+    build_dense_samples(r->rs, sh, r->stream);
   });
 }
 

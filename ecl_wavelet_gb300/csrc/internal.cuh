@@ -1,6 +1,7 @@
 // Host-side objects behind the opaque ewt_tree / ewt_rs handles, and the
 // functions the translation units share.
 #pragma once
+#include <atomic>
 #include <memory>
 #include <mutex>
 #include <vector>
@@ -19,9 +20,10 @@ using ecl::detail::TreeView;
 // do: arrays padded to 32-word multiples, total word count even.
 struct RSStore {
   std::vector<ArrayMeta> meta;  // host copy
-  DevBuf words, l1, l2, s0, s1, meta_d, jobs_d, rb;
+  DevBuf words, l1, l2, s0, s1, meta_d, jobs_d, rb, ds;
   uint64_t total_words = 0, total_l1 = 0, total_l2 = 0;
   uint64_t total_s0 = 0, total_s1 = 0;
+  uint32_t sel_shift = ecl::detail::kDefaultSelShift;  // dense sample rate
 
   // Lays out arrays of the given bit lengths and allocates words (zeroed),
   // L1, L2 and the device meta table.  Samples are allocated by build_rs.
@@ -29,7 +31,7 @@ struct RSStore {
   RSView view() const;
   uint64_t device_bytes() const {
     return words.bytes() + l1.bytes() + l2.bytes() + s0.bytes() + s1.bytes() + rb.bytes() +
-           meta_d.bytes();
+           ds.bytes() + meta_d.bytes();
   }
 };
 
@@ -41,9 +43,13 @@ void build_rs_counts(RSStore& rs, uint32_t first, uint32_t last,
 // Allocates and fills the select samples of every array (needs counts of
 // all arrays) and uploads the final meta table.
 void build_rs_samples(RSStore& rs, cudaStream_t stream);
-// Builds the query-side rank blocks of every array (needs the counts) and
-// uploads the meta table with their offsets.
+// Builds the query-side rank blocks of every array (needs the counts) and,
+// when rs.sel_shift > 0, the dense select samples in the same pass; uploads
+// the meta table with their offsets.
 void build_rank_blocks(RSStore& rs, cudaStream_t stream);
+// Rebuilds the dense select samples at rate 2^shift from the rank blocks
+// (shift 0 drops them: select then uses the reference-format samples).
+void build_dense_samples(RSStore& rs, uint32_t shift, cudaStream_t stream);
 
 struct QueryScratch {
   DevBuf in, out, types;
@@ -67,6 +73,10 @@ struct ewt_tree {
   // ewt_autotune: threads per CTA and resident CTAs per SM (0 = default)
   uint32_t tune_threads[4] = {0, 0, 0, 0};
   uint32_t tune_blocks[4] = {0, 0, 0, 0};
+  // set once the device view was copied out (ewt_get_device_view, a
+  // server): its pointers must stay valid, so the dense select samples are
+  // no longer rebuilt at another rate
+  mutable std::atomic<bool> view_shared{false};
   uint64_t n = 0, sigma = 0;
   uint32_t L = 0;
   bool is_min = false, pow2 = false;
@@ -89,6 +99,7 @@ struct ewt_tree {
 
 struct ewt_rs {
   int device = 0;
+  mutable std::atomic<bool> view_shared{false};  // as ewt_tree::view_shared
   ewt::RSStore rs;
   ewt::DevBuf err_d;
   std::mutex query_mu;

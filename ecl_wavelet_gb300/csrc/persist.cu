@@ -118,7 +118,8 @@ extern "C" int ewt_save(const ewt_tree* t, const char* path) {
     f.put_vec(t->level_bits);
     f.put_vec(t->rs.meta);
     for (uint64_t v : {t->rs.total_words, t->rs.total_l1, t->rs.total_l2,
-                       t->rs.total_s0, t->rs.total_s1})
+                       t->rs.total_s0, t->rs.total_s1,
+                       uint64_t(t->rs.ds.get() ? t->rs.sel_shift : 0)})
       f.put(v);
     PinnedBuf stage;
     stage.ensure(kPiece);
@@ -128,6 +129,7 @@ extern "C" int ewt_save(const ewt_tree* t, const char* path) {
     dev_to_file(f, t->rs.s0.get(), t->rs.s0.bytes(), stage, s);
     dev_to_file(f, t->rs.s1.get(), t->rs.s1.bytes(), stage, s);
     dev_to_file(f, t->rs.rb.get(), t->rs.rb.bytes(), stage, s);
+    dev_to_file(f, t->rs.ds.get(), t->rs.ds.bytes(), stage, s);
     dev_to_file(f, t->counts_d.get(), t->counts_d.bytes(), stage, s);
     dev_to_file(f, t->ranks_d.get(), t->ranks_d.bytes(), stage, s);
   });
@@ -179,6 +181,9 @@ extern "C" int ewt_load(const char* path, int gpu_index, ewt_tree** out) {
       t->rs.total_l2 = f.get();
       t->rs.total_s0 = f.get();
       t->rs.total_s1 = f.get();
+      t->rs.sel_shift = static_cast<uint32_t>(f.get());
+      EWT_REQUIRE(t->rs.sel_shift == 0 || (t->rs.sel_shift >= 5 && t->rs.sel_shift <= 16),
+                  EWT_ERR_INVALID_ARGUMENT, "index file is corrupt");
       PinnedBuf stage;
       stage.ensure(kPiece);
       uint64_t const big = t->n * 64 + (uint64_t(1) << 30);  // sanity bound
@@ -188,6 +193,9 @@ extern "C" int ewt_load(const char* path, int gpu_index, ewt_tree** out) {
       file_to_dev(f, t->rs.s0, stage, s, big);
       file_to_dev(f, t->rs.s1, stage, s, big);
       file_to_dev(f, t->rs.rb, stage, s, big);
+      file_to_dev(f, t->rs.ds, stage, s, big);
+      EWT_REQUIRE(t->rs.sel_shift == 0 || t->rs.ds.get() != nullptr,
+                  EWT_ERR_INVALID_ARGUMENT, "index file is corrupt");
       file_to_dev(f, t->counts_d, stage, s, (sig + 1) * 8);
       file_to_dev(f, t->ranks_d, stage, s, big);
       upload(t->rs.meta_d, t->rs.meta, s);

@@ -501,7 +501,30 @@ void autotune_typed(ewt_tree& t, uint64_t m, ewt_tuning* out) {
     t.tune_threads[kind] = 0;
     t.tune_blocks[kind] = 0;
     float const base = timed();
-    float best = base;
+    float sel_ms = base;
+    if (kind == 2 && !t.view_shared.load()) {
+      // dense select-sample rate first (select probes, default shape)
+      uint32_t const start = t.rs.ds.get() ? t.rs.sel_shift : 0;
+      uint32_t best_sh = start;
+      float best_ms = base;
+      for (uint32_t sh : {0u, 6u, 7u, 8u, 9u}) {
+        if (sh == start) continue;
+        build_dense_samples(t.rs, sh, s);
+        t.view.rs = t.rs.view();
+        float const ms = timed();
+        if (ms < best_ms) {
+          best_ms = ms;
+          best_sh = sh;
+        }
+      }
+      if (t.rs.sel_shift != best_sh || (best_sh && !t.rs.ds.get())) {
+        build_dense_samples(t.rs, best_sh, s);
+        t.view.rs = t.rs.view();
+      }
+      sel_ms = best_ms;
+    }
+    if (out) out->select_sample_rate = t.rs.ds.get() ? 1u << t.rs.sel_shift : 0u;
+    float best = sel_ms;  // select: at the kept sample rate
     uint32_t bt = 0, bb = 0;
     for (uint32_t th : thread_opts)
       for (uint32_t bl : block_opts) {

@@ -86,6 +86,10 @@ RSView RSStore::view() const {
         meta.back().rb_off + ceil_div(meta.back().bits, ecl::detail::kRankBlockBits);
     v.rbh = reinterpret_cast<uint64_t const*>(rb.as<unsigned char>() + blocks * 32);
   }
+  if (v.rb && ds.get()) {
+    v.ds = ds.as<uint32_t>();
+    v.sel_shift = sel_shift;
+  }
   v.num_arrays = static_cast<uint32_t>(meta.size());
   return v;
 }
@@ -322,36 +326,114 @@ void build_rs_samples(RSStore& rs, cudaStream_t stream) {
 
 namespace {
 
+using ecl::detail::kRankBlockBits;
+using ecl::detail::kRankBlockWords;
+
+__device__ __forceinline__ uint32_t owner_array(uint64_t const* start,
+                                                uint32_t num_arrays, uint64_t g) {
+  uint32_t lo = 0, hi = num_arrays - 1;
+  while (lo < hi) {
+    uint32_t const mid = (lo + hi + 1) >> 1;
+    if (start[mid] <= g) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Dense samples that fall in rank block b of array m: entry j names the
+// block holding the (j*R+1)-th zero / one, R = 2^sh.  ones = ones before the
+// block, w = its words (bits past the array end are not counted).
+__device__ __forceinline__ void put_dense_samples(uint32_t* __restrict__ ds,
+                                                  ArrayMeta const& m, uint64_t b,
+                                                  uint64_t ones,
+                                                  uint32_t const* w, uint32_t sh) {
+  uint64_t const pos = b * kRankBlockBits;
+  uint32_t const valid = static_cast<uint32_t>(
+      min(uint64_t(kRankBlockBits), m.bits - pos));
+  uint32_t c1 = 0;
+#pragma unroll
+  for (uint32_t j = 0; j < kRankBlockWords; ++j) {
+    uint32_t const lo = j * 32;
+    uint32_t const mask = valid >= lo + 32 ? ~0u
+                          : valid > lo     ? (1u << (valid - lo)) - 1u
+                                           : 0u;
+    c1 += __popc(w[j] & mask);
+  }
+  uint64_t const R = uint64_t(1) << sh;
+  uint32_t const blk = static_cast<uint32_t>(b);
+#pragma unroll
+  for (int val = 0; val < 2; ++val) {
+    uint64_t const before = val ? ones : pos - ones;
+    uint32_t const c = val ? c1 : valid - c1;
+    if (c == 0) continue;
+    uint32_t* S = ds + (val ? m.ds1_off : m.ds0_off);
+    uint64_t const entries = ((val ? m.ones : m.bits - m.ones) + R - 1) >> sh;
+    uint64_t const last = min((before + c - 1) >> sh, entries - 1);
+    for (uint64_t j = (before + R - 1) >> sh; j <= last && entries; ++j)
+      S[j] = blk;
+  }
+}
+
 // One thread per rank block (32-byte sector) of every array: the low word
 // of the ones before the block (from the L1/L2 counts) and the block's 7
 // words; the first block of every 2^24 also writes the full count to the
-// high-count table.
+// high-count table, and with ds set the block's dense select samples.
 __global__ void __launch_bounds__(256)
 rank_blocks_kernel(RSView v, uint64_t const* __restrict__ line_start,
                    uint32_t num_arrays, uint64_t total_lines,
                    uint64_t total_words, uint4* __restrict__ out,
-                   uint64_t* __restrict__ high) {
+                   uint64_t* __restrict__ high, uint32_t* __restrict__ ds,
+                   uint32_t sel_shift) {
   uint64_t const g = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   if (g >= total_lines) return;
-  uint32_t lo = 0, hi = num_arrays - 1;
-  while (lo < hi) {
-    uint32_t const mid = (lo + hi + 1) >> 1;
-    if (line_start[mid] <= g) lo = mid; else hi = mid - 1;
-  }
-  ArrayMeta const m = v.meta[lo];
-  uint64_t const b = g - line_start[lo];
-  uint64_t const pos = b * ecl::detail::kRankBlockBits;
+  uint32_t const a = owner_array(line_start, num_arrays, g);
+  ArrayMeta const m = v.meta[a];
+  uint64_t const b = g - line_start[a];
+  uint64_t const pos = b * kRankBlockBits;
   uint64_t const ones = ecl::detail::rs_rank1<false>(v, m, pos, nullptr);
-  uint64_t const w0 = m.word_off + b * ecl::detail::kRankBlockWords;
-  uint32_t w[ecl::detail::kRankBlockWords];
+  uint64_t const w0 = m.word_off + b * kRankBlockWords;
+  uint32_t w[kRankBlockWords];
 #pragma unroll
-  for (uint32_t j = 0; j < ecl::detail::kRankBlockWords; ++j)
+  for (uint32_t j = 0; j < kRankBlockWords; ++j)
     w[j] = w0 + j < total_words ? v.words[w0 + j] : 0u;
   uint4* line = out + g * 2;
   line[0] = make_uint4(static_cast<uint32_t>(ones), w[0], w[1], w[2]);
   line[1] = make_uint4(w[3], w[4], w[5], w[6]);
   if ((b & ((uint64_t(1) << ecl::detail::kRankHighShift) - 1)) == 0)
     high[m.rbh_off + (b >> ecl::detail::kRankHighShift)] = ones;
+  if (ds) put_dense_samples(ds, m, b, ones, w, sel_shift);
+}
+
+// Dense select samples at a new rate from the finished rank blocks.
+__global__ void __launch_bounds__(256)
+dense_samples_kernel(RSView v, uint64_t const* __restrict__ line_start,
+                     uint32_t num_arrays, uint64_t total_lines,
+                     uint32_t* __restrict__ ds, uint32_t sel_shift) {
+  uint64_t const g = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (g >= total_lines) return;
+  uint32_t const a = owner_array(line_start, num_arrays, g);
+  ArrayMeta const m = v.meta[a];
+  uint64_t const b = g - line_start[a];
+  uint4 const q0 = v.rb[g * 2], q1 = v.rb[g * 2 + 1];
+  uint32_t const w[kRankBlockWords] = {q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+  uint64_t const ones = ecl::detail::rb_ones_before(v, m, b, q0.x);
+  put_dense_samples(ds, m, b, ones, w, sel_shift);
+}
+
+// Lays out the dense samples of every array at rate 2^shift (offsets into
+// the meta table) and allocates them; returns false for shift 0.
+bool layout_dense(RSStore& rs, uint32_t shift) {
+  rs.ds.reset();
+  rs.sel_shift = shift;
+  if (shift == 0) return false;
+  uint64_t total = 0;
+  for (auto& m : rs.meta) {
+    m.ds1_off = total;
+    total += ceil_div(m.ones, uint64_t(1) << shift);
+    m.ds0_off = total;
+    total += ceil_div(m.bits - m.ones, uint64_t(1) << shift);
+  }
+  rs.ds.alloc(std::max<uint64_t>(total, 1) * 4);
+  return true;
 }
 
 }  // namespace
@@ -371,6 +453,7 @@ void build_rank_blocks(RSStore& rs, cudaStream_t stream) {
   }
   // blocks, then the high-count table in the same allocation
   rs.rb.alloc(total * 32 + highs * 8);
+  bool const dense = layout_dense(rs, rs.sel_shift);
   DevBuf start_d(count * 8);
   EWT_CUDA(cudaMemcpyAsync(start_d.get(), start.data(), count * 8,
                            cudaMemcpyHostToDevice, stream));
@@ -379,13 +462,45 @@ void build_rank_blocks(RSStore& rs, cudaStream_t stream) {
                            stream));
   RSView v = rs.view();
   v.rb = nullptr;  // headers come from the L1/L2 counts
+  v.ds = nullptr;
+  v.sel_shift = 0;
   {
     PhaseTimer pt(EWT_PHASE_SAMPLES, stream);
     rank_blocks_kernel<<<static_cast<uint32_t>(ceil_div(total, 256)), 256, 0,
                          stream>>>(v, start_d.as<uint64_t>(), count, total,
                                    rs.total_words, rs.rb.as<uint4>(),
                                    reinterpret_cast<uint64_t*>(
-                                       rs.rb.as<unsigned char>() + total * 32));
+                                       rs.rb.as<unsigned char>() + total * 32),
+                                   dense ? rs.ds.as<uint32_t>() : nullptr,
+                                   rs.sel_shift);
+    EWT_LAUNCHED();
+  }
+  EWT_CUDA(cudaStreamSynchronize(stream));
+}
+
+void build_dense_samples(RSStore& rs, uint32_t shift, cudaStream_t stream) {
+  EWT_REQUIRE(shift == 0 || (shift >= 5 && shift <= 16), EWT_ERR_INVALID_ARGUMENT,
+              "dense select sample rate must be 2^5 .. 2^16");
+  EWT_CUDA(cudaStreamSynchronize(stream));  // no query may read the old ones
+  uint32_t const count = static_cast<uint32_t>(rs.meta.size());
+  if (!layout_dense(rs, shift) || count == 0 || !rs.rb.get()) {
+    rs.ds.reset();
+    return;
+  }
+  std::vector<uint64_t> start(count);
+  for (uint32_t a = 0; a < count; ++a) start[a] = rs.meta[a].rb_off;
+  uint64_t const total = rs.meta.back().rb_off +
+                         ceil_div(rs.meta.back().bits, kRankBlockBits);
+  DevBuf start_d(count * 8);
+  EWT_CUDA(cudaMemcpyAsync(start_d.get(), start.data(), count * 8,
+                           cudaMemcpyHostToDevice, stream));
+  EWT_CUDA(cudaMemcpyAsync(rs.meta_d.get(), rs.meta.data(),
+                           count * sizeof(ArrayMeta), cudaMemcpyHostToDevice,
+                           stream));
+  if (total > 0) {
+    dense_samples_kernel<<<static_cast<uint32_t>(ceil_div(total, 256)), 256, 0,
+                           stream>>>(rs.view(), start_d.as<uint64_t>(), count,
+                                     total, rs.ds.as<uint32_t>(), shift);
     EWT_LAUNCHED();
   }
   EWT_CUDA(cudaStreamSynchronize(stream));

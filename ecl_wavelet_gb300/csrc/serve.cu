@@ -278,6 +278,7 @@ uint32_t register_tree(ewt_server* S, ewt_tree* t, bool owned) {
   EWT_REQUIRE(t->device == S->device, EWT_ERR_INVALID_ARGUMENT,
               "the tree lives on another GPU");
   uint32_t const id = static_cast<uint32_t>(S->trees.size());
+  t->view_shared.store(true);
   EWT_CUDA(cudaMemcpy(S->views_d + id, &t->view, sizeof(TreeView), cudaMemcpyHostToDevice));
   S->trees.push_back(t);
   S->owned.push_back(owned);

@@ -45,6 +45,8 @@ struct ArrayMeta {
   uint64_t num_last_l2; // L2 blocks inside the last L1 block
   uint64_t rb_off;      // first rank block (32-byte sector) of the array
   uint64_t rbh_off;     // first high-count entry of the array
+  uint64_t ds0_off;     // first dense zero-sample (rank-block index, u32)
+  uint64_t ds1_off;     // first dense one-sample
 };
 
 /* Query-side rank blocks: each 32-byte block (one DRAM sector) holds the low
@@ -59,6 +61,14 @@ constexpr uint64_t kRankBlockBits = 224;
 constexpr uint64_t kRankBlockWords = kRankBlockBits / 32;
 constexpr uint32_t kRankHighShift = 24;
 
+/* Dense select samples (query side, next to the rank blocks): for every
+ * R-th zero / one (R = 2^sel_shift; entry j covers the (j*R+1)-th) the index
+ * of the rank block holding it, relative to the array's first block.  A
+ * select reads two neighbouring entries, which bracket its block, and then
+ * one or two rank blocks; sel_shift = 0 means none were built and select
+ * uses the reference-format samples and counts. */
+constexpr uint32_t kDefaultSelShift = 7;
+
 /* A set of bit arrays with rank/select support, all in device memory. */
 struct RSView {
   const uint32_t* words;
@@ -69,8 +79,9 @@ struct RSView {
   const ArrayMeta* meta;  // device array of num_arrays entries
   const uint4* rb;        // rank blocks (2 uint4 per block), may be null
   const uint64_t* rbh;    // high counts of the rank blocks
+  const uint32_t* ds;     // dense select samples (ArrayMeta::ds0/ds1_off)
   uint32_t num_arrays;
-  uint32_t reserved;
+  uint32_t sel_shift;     // log2 of the dense sample rate; 0 = none
 };
 
 /* Everything a query walk needs; trivially copyable into a kernel. */
@@ -130,6 +141,17 @@ __device__ __forceinline__ bool rs_bit(const RSView& v, const ArrayMeta& m,
   return (__ldg(v.words + m.word_off + (pos >> 5)) >> (pos & 31)) & 1u;
 }
 
+/* Ones before rank block k of an array whose header holds the low word lo:
+ * the high part comes from the high-count table for k >= 2^24. */
+__device__ __forceinline__ uint64_t rb_ones_before(const RSView& v,
+                                                   const ArrayMeta& m,
+                                                   uint64_t k, uint32_t lo) {
+  uint64_t const hj = k >> kRankHighShift;
+  if (!hj) return lo;
+  uint64_t const h = __ldg(v.rbh + m.rbh_off + hj);
+  return h + static_cast<uint32_t>(lo - static_cast<uint32_t>(h));
+}
+
 /* Ones in [0, pos) of one array, pos <= bits; with GetBit also the bit at
  * pos (false for pos == bits).  Loads the L1 entry, the L2 entry and the
  * 128-bit chunks of the 512-bit block up to pos, all independent. */
@@ -159,13 +181,7 @@ __device__ __forceinline__ uint64_t rs_rank1(const RSView& v,
     }
     acc += __popc(cur & ((1u << (off & 31)) - 1u));
     if (GetBit) *bit = (cur >> (off & 31)) & 1u;
-    uint64_t before = q0.x;
-    uint64_t const hj = blk >> kRankHighShift;
-    if (hj) {
-      uint64_t const h = __ldg(v.rbh + m.rbh_off + hj);
-      before = h + static_cast<uint32_t>(q0.x - static_cast<uint32_t>(h));
-    }
-    return before + acc;
+    return rb_ones_before(v, m, blk, q0.x) + acc;
   }
   uint64_t const b2 = pos >> 9;
   uint64_t r = __ldg(v.l1 + m.l1_off + (pos >> 16));
@@ -194,14 +210,73 @@ __device__ __forceinline__ uint64_t rs_rank1(const RSView& v,
   return r + acc;
 }
 
+/* rs_select through the dense samples and rank blocks, 0 < i <= total:
+ * two sample entries bracket the rank block holding the i-th `Value` bit;
+ * a binary search over block headers narrows wider brackets to two blocks,
+ * both read at once; the block whose count before it is below i holds it. */
+template <int Value>
+__device__ __forceinline__ uint64_t rs_select_dense(const RSView& v,
+                                                    const ArrayMeta& m,
+                                                    uint64_t i, uint64_t total) {
+  uint32_t const* S = v.ds + (Value ? m.ds1_off : m.ds0_off);
+  uint32_t const sh = v.sel_shift;
+  uint64_t const j = (i - 1) >> sh;
+  uint64_t const nblk = (m.bits + kRankBlockBits - 1) / kRankBlockBits;
+  // entries name blocks of this array; the clamps keep every read inside it
+  uint64_t lo = min(uint64_t(__ldg(S + j)), nblk - 1);
+  uint64_t hi = ((j + 1) << sh) < total ? __ldg(S + j + 1) : nblk - 1;
+  hi = min(max(hi, lo), nblk - 1);
+  uint4 const* rb = v.rb + m.rb_off * 2;
+  // value bits before block k given its header word
+  auto before = [&](uint64_t k, uint32_t h) -> uint64_t {
+    uint64_t const ones = rb_ones_before(v, m, k, h);
+    return Value ? ones : k * kRankBlockBits - ones;
+  };
+  while (hi - lo > 1) {  // wide brackets only (sparse values)
+    uint64_t const mid = (lo + hi + 1) >> 1;
+    uint32_t const h = __ldg(reinterpret_cast<uint32_t const*>(rb + mid * 2));
+    if (before(mid, h) < i) lo = mid; else hi = mid - 1;
+  }
+  uint4 const a0 = __ldg(rb + lo * 2), a1 = __ldg(rb + lo * 2 + 1);
+  uint4 const c0 = __ldg(rb + hi * 2), c1 = __ldg(rb + hi * 2 + 1);
+  uint64_t const bh = before(hi, c0.x);
+  bool const in_hi = hi > lo && bh < i;
+  uint4 const b0 = in_hi ? c0 : a0, b1 = in_hi ? c1 : a1;
+  uint64_t const t = in_hi ? hi : lo;
+  uint64_t const bt = in_hi ? bh : before(lo, a0.x);
+  uint32_t r = static_cast<uint32_t>(i - bt);  // 1 ..= kRankBlockBits
+  uint32_t const w[kRankBlockWords] = {b0.y, b0.z, b0.w, b1.x,
+                                       b1.y, b1.z, b1.w};
+  uint32_t sel = 0, wj = 0;
+  bool found = false;
+#pragma unroll
+  for (uint32_t q = 0; q < kRankBlockWords; ++q) {
+    uint32_t const x = Value ? w[q] : ~w[q];
+    uint32_t const c = __popc(x);
+    if (!found) {
+      if (r <= c) {
+        found = true;
+        sel = x;
+        wj = q;
+      } else {
+        r -= c;
+      }
+    }
+  }
+  if (!found) return m.bits;  // not reached for valid structures
+  return t * kRankBlockBits + wj * 32 + select_in_word(sel, r);
+}
+
 /* Position of the i-th (1-based) `Value` bit, or bits when there are fewer
- * (or i == 0).  Sample bracket -> L1 binary search -> L2 binary search in
- * the bracketed range -> scan of the 512-bit block -> in-word select. */
+ * (or i == 0).  With dense samples: rs_select_dense.  Otherwise sample
+ * bracket -> L1 binary search -> L2 binary search in the bracketed range ->
+ * scan of the 512-bit block -> in-word select. */
 template <int Value>
 __device__ __forceinline__ uint64_t rs_select(const RSView& v,
                                               const ArrayMeta& m, uint64_t i) {
   uint64_t const total = Value ? m.ones : m.bits - m.ones;
   if (i == 0 || i > total) return m.bits;
+  if (v.sel_shift) return rs_select_dense<Value>(v, m, i, total);
   uint64_t const* S = Value ? v.s1 + m.s1_off : v.s0 + m.s0_off;
   uint64_t const q = i / kSampleRate;
   uint64_t const lo = q ? __ldg(S + q - 1) : 0;

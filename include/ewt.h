@@ -216,19 +216,36 @@ int ewt_abi_version(void);
 uint64_t ewt_launch_count(void);
 
 /* ---- autotuning -----------------------------------------------------------
- * Times the query kernels of every kind (access, rank, select, mixed) on
- * probe_queries device-generated valid queries over this tree for candidate
- * launch shapes (threads per CTA x resident CTAs per SM) and keeps the
- * fastest per kind for every later launch on this tree; *out (may be NULL)
- * reports the choice and the default and tuned rates.  Results never
- * depend on the launch shape.  No reference counterpart (the reference's
- * launch configuration is fixed per call site, utils.cu:42-94). */
+ * Times the query kernels on probe_queries device-generated valid queries
+ * over this tree and keeps the fastest configuration for every later query
+ * on it: first the dense select-sample rate (every R-th zero / one, R in
+ * {64, 128, 256, 512}, or none: the reference-format samples alone), timed
+ * on select probes, then per kind (access, rank, select, mixed) the launch
+ * shape (threads per CTA x resident CTAs per SM).  *out (may be NULL)
+ * reports the choices and the default and tuned rates.  Results never
+ * depend on either choice.  Once the tree's device view was copied out
+ * (ewt_get_device_view, ewt_server_add_tree) the sample rate stays as it is,
+ * so that view stays valid.  No reference counterpart (the reference fixes
+ * its launch configuration per call site, utils.cu:42-94, and its sample
+ * rate at compile time, rank_select.cuh:44-64). */
 typedef struct ewt_tuning {
   uint32_t threads[4];       /* threads per CTA: access, rank, select, mixed */
   uint32_t blocks_per_sm[4]; /* resident CTAs per SM; 0 = as many as fit    */
+  uint32_t select_sample_rate; /* R of the dense select samples; 0 = none  */
+  uint32_t reserved;
   double default_mq_s[4], tuned_mq_s[4];
 } ewt_tuning;
 int ewt_autotune(ewt_tree* tree, uint64_t probe_queries, ewt_tuning* out);
+
+/* Rebuilds the dense select samples (query side, beside the reference-format
+ * samples, which exports keep) at one entry per `rate` zeros / ones: 0 drops
+ * them (select then runs the reference's sample -> L1 -> L2 search), else a
+ * power of two in [32, 65536]; each entry costs 4 bytes.  Built at 128 by
+ * default.  Refused (EWT_ERR_INVALID_ARGUMENT) once the device view was
+ * copied out.  No reference counterpart (rank_select.cuh:44-64 fixes one
+ * sample per 4096 at compile time). */
+int ewt_set_select_samples(ewt_tree* tree, uint32_t rate);
+int ewt_rs_set_select_samples(ewt_rs* rs, uint32_t rate);
 
 /* ---- index files --------------------------------------------------------
  * Writes a built tree (shape, level bits, RankSelect counts and samples,

@@ -152,8 +152,11 @@ def test_autotuned_queries_exact(ewt, oracle, dtype, sigma, minimal):
     text, alphabet = random_text(rng, 300_000, sigma, dtype, minimal=minimal)
     gt = ewt.WaveletTree(text, alphabet)
     tuning = gt.autotune(1 << 14)
-    assert set(tuning) == {"access", "rank", "select", "mixed"}
-    for kind, r in tuning.items():
+    assert set(tuning) == {"access", "rank", "select", "mixed",
+                           "select_sample_rate"}
+    assert tuning["select_sample_rate"] in (0, 64, 128, 256, 512)
+    for kind in ("access", "rank", "select", "mixed"):
+        r = tuning[kind]
         assert r["threads"] in (128, 256), (kind, r)
         assert r["blocks_per_sm"] in (0, 2, 4, 6, 8), (kind, r)
         assert r["tuned_mq_s"] >= r["default_mq_s"] > 0, (kind, r)
@@ -162,3 +165,48 @@ def test_autotuned_queries_exact(ewt, oracle, dtype, sigma, minimal):
     check_queries(gt, ot, text, al, 20_000, seed=9)
     with pytest.raises(ewt.EwtError):
         gt.autotune(10)  # below the probe minimum
+
+
+@pytest.mark.parametrize("rate", [0, 32, 64, 512, 65536])
+def test_select_sample_rates_exact(ewt, oracle, rate):
+    """Select through dense samples at every rate (and through the
+    reference-format samples alone, rate 0) equals the plain scan, on a
+    Zipf text whose deep levels hold long runs of one bit value (wide
+    sample brackets, the binary-search path) next to dense ones."""
+    from tests.workloads import random_text
+    rng = np.random.default_rng(rate + 3)
+    text, alphabet = random_text(rng, 400_000, 200, np.uint8, minimal=False,
+                                 zipf=1.6)
+    gt = ewt.WaveletTree(text, alphabet)
+    gt.set_select_samples(rate)
+    ot = oracle.OracleTree(text, alphabet)
+    check_queries(gt, ot, text, np.asarray(alphabet, dtype=np.uint64), 20_000,
+                  seed=rate)
+    with pytest.raises(ewt.EwtError):
+        gt.set_select_samples(48)  # not a power of two
+
+
+@pytest.mark.parametrize("rate", [0, 32, 128, 4096])
+def test_rs_select_sample_rates_exact(ewt, oracle, rate):
+    """Standalone RankSelect: select0/select1 at every dense sample rate on
+    iid, sparse (a few ones in a million bits), dense and empty arrays."""
+    rng = np.random.default_rng(rate + 11)
+    sizes = [1_000_003, 999_999, 777_777, 600_000, 4_095, 1]
+    words = [rng.integers(0, 2**32, (s + 31) // 32, dtype=np.uint64).astype(np.uint32)
+             for s in sizes]
+    words[1][:] = 0
+    words[1][rng.integers(0, words[1].size, 40)] = np.uint32(1 << 7)
+    words[2] |= np.uint32(0xFFFFFFFE)
+    words[3][:] = 0
+    g = ewt.RankSelect(words, sizes)
+    g.set_select_samples(rate)
+    o = oracle.OracleRS(words, sizes)
+    ones = g.export("TOTAL_ONES").astype(np.int64)
+    for a, bits in enumerate(sizes):
+        for v in (0, 1):
+            tot = int(ones[a]) if v else bits - int(ones[a])
+            ks = np.concatenate([rng.integers(1, tot + 1, 3000) if tot else
+                                 np.array([], np.int64),
+                                 np.array([1, max(tot, 1), tot + 1])])
+            assert np.array_equal(g.select(a, v, ks),
+                                  o.select_batch(a, ks, v)), (a, v)
