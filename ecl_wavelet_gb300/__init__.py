@@ -142,7 +142,7 @@ SIGNATURES = {
 }
 
 PHASES = ["hist", "fill", "rs_counts", "split", "node_ranks", "samples",
-          "query", "h2d"]
+          "query", "h2d", "quad"]
 
 
 class PhaseTimes(C.Structure):

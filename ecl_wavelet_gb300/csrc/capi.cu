@@ -165,7 +165,7 @@ void count_launch(uint64_t k) { g_launches.fetch_add(k, std::memory_order_relaxe
 }  // namespace ewt
 
 uint64_t ewt_tree::device_bytes() const {
-  return rs.device_bytes() + counts_d.bytes() + ranks_d.bytes() +
+  return rs.device_bytes() + quad.bytes() + counts_d.bytes() + ranks_d.bytes() +
          node_base_d.bytes() + nodes_at_level_d.bytes() + code_len_d.bytes() +
          code_bits_d.bytes() + alphabet_d.bytes() + err_d.bytes();
 }
@@ -686,8 +686,7 @@ int ewt_set_select_samples(ewt_tree* t, uint32_t rate) {
                 "the tree's device view was copied out; its samples stay");
     DeviceGuard g(t->device);
     AllocStream as(t->stream);
-    build_dense_samples(t->rs, sh, t->stream);
-    t->view.rs = t->rs.view();
+    set_select_rate(*t, sh, t->stream);
   });
 }
 

@@ -24,6 +24,7 @@ struct RSStore {
   uint64_t total_words = 0, total_l1 = 0, total_l2 = 0;
   uint64_t total_s0 = 0, total_s1 = 0;
   uint32_t sel_shift = ecl::detail::kDefaultSelShift;  // dense sample rate
+  std::vector<uint8_t> skip_blocks;  // arrays built without rank blocks
 
   // Lays out arrays of the given bit lengths and allocates words (zeroed),
   // L1, L2 and the device meta table.  Samples are allocated by build_rs.
@@ -47,9 +48,25 @@ void build_rs_samples(RSStore& rs, cudaStream_t stream);
 // when rs.sel_shift > 0, the dense select samples in the same pass; uploads
 // the meta table with their offsets.
 void build_rank_blocks(RSStore& rs, cudaStream_t stream);
+// Rank-block start of every array (running totals; arrays without blocks
+// add none) and the total block count.
+uint64_t rank_block_starts(std::vector<ArrayMeta> const& meta,
+                           std::vector<uint64_t>& start);
 // Rebuilds the dense select samples at rate 2^shift from the rank blocks
 // (shift 0 drops them: select then uses the reference-format samples).
 void build_dense_samples(RSStore& rs, uint32_t shift, cudaStream_t stream);
+
+// Quad query levels of a power-of-two tree (quad.cu).
+struct QuadStore {
+  std::vector<ecl::detail::QuadLevel> levels;  // host copy
+  DevBuf blocks, sb, ds, node_ranks, levels_d;
+  uint32_t sel_shift = ecl::detail::kDefaultSelShift;
+  ecl::detail::QuadView view() const;
+  uint64_t bytes() const {
+    return blocks.bytes() + sb.bytes() + ds.bytes() + node_ranks.bytes() +
+           levels_d.bytes();
+  }
+};
 
 struct QueryScratch {
   DevBuf in, out, types;
@@ -88,6 +105,7 @@ struct ewt_tree {
   std::vector<ewt::NodeInfoH> nodes;
   std::vector<uint64_t> nodes_at_level, node_base, level_bits;
   ewt::RSStore rs;
+  ewt::QuadStore quad;
   ewt::DevBuf counts_d, ranks_d, node_base_d, nodes_at_level_d, code_len_d,
       code_bits_d, alphabet_d, err_d;
   ecl::detail::TreeView view{};
@@ -145,6 +163,16 @@ void launch_serve_items(uint32_t elem_size, TreeView const* d_views,
                         void const* reqs, void const* items, uint32_t num_items,
                         uint32_t max_levels, uint32_t* req_err, cudaStream_t s);
 void prepare_serve_kernels(uint32_t elem_size);
+// Quad query levels (quad.cu): whether a tree gets them (power-of-two
+// alphabet, two or more levels), their build from the finished binary levels
+// and count table C (sigma + 1 entries), and a rebuild of their dense select
+// samples at rate 2^shift (0: none).
+bool quad_eligible(ewt_tree const& t);
+void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, cudaStream_t st);
+void build_quad_samples(ewt_tree& t, uint32_t shift, cudaStream_t st);
+// Dense select samples of the binary and quad levels at rate 2^shift (0:
+// none), and the tree's view updated.
+void set_select_rate(ewt_tree& t, uint32_t shift, cudaStream_t st);
 // Times candidate launch shapes of every query kind on probe queries and
 // keeps the fastest in the tree (queries.cu).
 void autotune_queries(ewt_tree& t, uint64_t probe_queries, ewt_tuning* out);

@@ -132,6 +132,15 @@ extern "C" int ewt_save(const ewt_tree* t, const char* path) {
     dev_to_file(f, t->rs.ds.get(), t->rs.ds.bytes(), stage, s);
     dev_to_file(f, t->counts_d.get(), t->counts_d.bytes(), stage, s);
     dev_to_file(f, t->ranks_d.get(), t->ranks_d.bytes(), stage, s);
+    // quad query levels (none for other alphabets)
+    f.put_vec(t->quad.levels);
+    f.put(t->quad.ds.get() ? t->quad.sel_shift : 0);
+    if (!t->quad.levels.empty()) {
+      dev_to_file(f, t->quad.blocks.get(), t->quad.blocks.bytes(), stage, s);
+      dev_to_file(f, t->quad.sb.get(), t->quad.sb.bytes(), stage, s);
+      dev_to_file(f, t->quad.ds.get(), t->quad.ds.bytes(), stage, s);
+      dev_to_file(f, t->quad.node_ranks.get(), t->quad.node_ranks.bytes(), stage, s);
+    }
   });
 }
 
@@ -198,6 +207,21 @@ extern "C" int ewt_load(const char* path, int gpu_index, ewt_tree** out) {
                   EWT_ERR_INVALID_ARGUMENT, "index file is corrupt");
       file_to_dev(f, t->counts_d, stage, s, (sig + 1) * 8);
       file_to_dev(f, t->ranks_d, stage, s, big);
+      t->quad.levels = f.get_vec<ecl::detail::QuadLevel>(t->L / 2 + 1);
+      t->quad.sel_shift = static_cast<uint32_t>(f.get());
+      EWT_REQUIRE(t->quad.levels.empty() ||
+                      (t->quad.levels.size() == t->L / 2 && quad_eligible(*t) &&
+                       (t->quad.sel_shift == 0 ||
+                        (t->quad.sel_shift >= 5 && t->quad.sel_shift <= 16))),
+                  EWT_ERR_INVALID_ARGUMENT, "index file is corrupt");
+      if (!t->quad.levels.empty()) {
+        file_to_dev(f, t->quad.blocks, stage, s, big);
+        file_to_dev(f, t->quad.sb, stage, s, big);
+        file_to_dev(f, t->quad.ds, stage, s, big);
+        file_to_dev(f, t->quad.node_ranks, stage, s, big);
+        upload(t->quad.levels_d, t->quad.levels, s);
+        if (t->quad.sel_shift == 0) t->quad.ds.reset();
+      }
       upload(t->rs.meta_d, t->rs.meta, s);
       upload(t->node_base_d, t->node_base, s);
       upload(t->nodes_at_level_d, t->nodes_at_level, s);

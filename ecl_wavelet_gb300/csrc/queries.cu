@@ -509,18 +509,15 @@ void autotune_typed(ewt_tree& t, uint64_t m, ewt_tuning* out) {
       float best_ms = base;
       for (uint32_t sh : {0u, 6u, 7u, 8u, 9u}) {
         if (sh == start) continue;
-        build_dense_samples(t.rs, sh, s);
-        t.view.rs = t.rs.view();
+        set_select_rate(t, sh, s);
         float const ms = timed();
         if (ms < best_ms) {
           best_ms = ms;
           best_sh = sh;
         }
       }
-      if (t.rs.sel_shift != best_sh || (best_sh && !t.rs.ds.get())) {
-        build_dense_samples(t.rs, best_sh, s);
-        t.view.rs = t.rs.view();
-      }
+      if (t.rs.sel_shift != best_sh || (best_sh && !t.rs.ds.get()))
+        set_select_rate(t, best_sh, s);
       sel_ms = best_ms;
     }
     if (out) out->select_sample_rate = t.rs.ds.get() ? 1u << t.rs.sel_shift : 0u;

@@ -43,7 +43,8 @@ void RSStore::layout(std::vector<uint64_t> const& bits) {
     total_l2 += (m.num_l1 - 1) * kL2PerL1 + m.num_last_l2;
   }
   total_words += total_words % 2;
-  words.alloc(total_words * 4);
+  // 16 words of slack: readers may fetch one word past an array's end
+  words.alloc(total_words * 4 + 64);
   l1.alloc(total_l1 * 8);
   l2.alloc(total_l2 * 2);
   meta_d.alloc(meta.size() * sizeof(ArrayMeta));
@@ -82,8 +83,8 @@ RSView RSStore::view() const {
   v.meta = meta_d.as<ArrayMeta>();
   v.rb = rb.get() ? rb.as<uint4>() : nullptr;
   if (v.rb && !meta.empty()) {  // the high-count table follows the blocks
-    uint64_t const blocks =
-        meta.back().rb_off + ceil_div(meta.back().bits, ecl::detail::kRankBlockBits);
+    std::vector<uint64_t> start;
+    uint64_t const blocks = rank_block_starts(meta, start);
     v.rbh = reinterpret_cast<uint64_t const*>(rb.as<unsigned char>() + blocks * 32);
   }
   if (v.rb && ds.get()) {
@@ -427,6 +428,10 @@ bool layout_dense(RSStore& rs, uint32_t shift) {
   if (shift == 0) return false;
   uint64_t total = 0;
   for (auto& m : rs.meta) {
+    if (m.rb_off == ecl::detail::kNoBlocks) {
+      m.ds0_off = m.ds1_off = ecl::detail::kNoBlocks;
+      continue;
+    }
     m.ds1_off = total;
     total += ceil_div(m.ones, uint64_t(1) << shift);
     m.ds0_off = total;
@@ -438,14 +443,30 @@ bool layout_dense(RSStore& rs, uint32_t shift) {
 
 }  // namespace
 
+uint64_t rank_block_starts(std::vector<ArrayMeta> const& meta,
+                           std::vector<uint64_t>& start) {
+  start.assign(meta.size(), 0);
+  uint64_t total = 0;
+  for (size_t a = 0; a < meta.size(); ++a) {
+    start[a] = total;
+    if (meta[a].rb_off != ecl::detail::kNoBlocks)
+      total += ceil_div(meta[a].bits, kRankBlockBits);
+  }
+  return total;
+}
+
 void build_rank_blocks(RSStore& rs, cudaStream_t stream) {
   uint32_t const count = static_cast<uint32_t>(rs.meta.size());
   std::vector<uint64_t> start(count);
   uint64_t total = 0, highs = 0;
   for (uint32_t a = 0; a < count; ++a) {
+    start[a] = total;
+    if (a < rs.skip_blocks.size() && rs.skip_blocks[a]) {
+      rs.meta[a].rb_off = rs.meta[a].rbh_off = ecl::detail::kNoBlocks;
+      continue;
+    }
     rs.meta[a].rb_off = total;
     rs.meta[a].rbh_off = highs;
-    start[a] = total;
     uint64_t const blocks = ceil_div(rs.meta[a].bits, ecl::detail::kRankBlockBits);
     total += blocks;
     highs += ceil_div(std::max<uint64_t>(blocks, 1),
@@ -464,7 +485,7 @@ void build_rank_blocks(RSStore& rs, cudaStream_t stream) {
   v.rb = nullptr;  // headers come from the L1/L2 counts
   v.ds = nullptr;
   v.sel_shift = 0;
-  {
+  if (total > 0) {
     PhaseTimer pt(EWT_PHASE_SAMPLES, stream);
     rank_blocks_kernel<<<static_cast<uint32_t>(ceil_div(total, 256)), 256, 0,
                          stream>>>(v, start_d.as<uint64_t>(), count, total,
@@ -487,10 +508,8 @@ void build_dense_samples(RSStore& rs, uint32_t shift, cudaStream_t stream) {
     rs.ds.reset();
     return;
   }
-  std::vector<uint64_t> start(count);
-  for (uint32_t a = 0; a < count; ++a) start[a] = rs.meta[a].rb_off;
-  uint64_t const total = rs.meta.back().rb_off +
-                         ceil_div(rs.meta.back().bits, kRankBlockBits);
+  std::vector<uint64_t> start;
+  uint64_t const total = rank_block_starts(rs.meta, start);
   DevBuf start_d(count * 8);
   EWT_CUDA(cudaMemcpyAsync(start_d.get(), start.data(), count * 8,
                            cudaMemcpyHostToDevice, stream));

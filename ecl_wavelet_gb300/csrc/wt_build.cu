@@ -788,8 +788,13 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
     }
   }
   build_rs_samples(t.rs, st);
+  // binary levels that quad levels cover get no rank blocks
+  t.rs.skip_blocks.assign(L, 0);
+  if (quad_eligible(t))
+    for (uint32_t l = 0; l < (L & ~1u); ++l) t.rs.skip_blocks[l] = 1;
   build_rank_blocks(t.rs, st);
   v.rs = t.rs.view();
+  v.quad = ecl::detail::QuadView{};
   uint32_t build_err = 0;
   EWT_CUDA(cudaMemcpyAsync(&build_err, err_build, 4, cudaMemcpyDeviceToHost,
                            st));
@@ -805,6 +810,8 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   t.counts.assign(c.begin(), c.begin() + sigma);
   t.occ.resize(sigma);
   for (uint64_t i = 0; i < sigma; ++i) t.occ[i] = c[i + 1] - c[i];
+  build_quad(t, c, st);
+  v.quad = t.quad.view();
 }
 
 }  // namespace
@@ -828,6 +835,7 @@ void fill_tree_view(ewt_tree& t) {
   v.elem_size = t.elem_size;
   v.is_pow2 = t.pow2;
   v.is_min = t.is_min;
+  v.quad = t.quad.view();
 }
 
 void build_tree(ewt_tree& t, const void* data, uint64_t n, int elem_size,

@@ -69,6 +69,10 @@ constexpr uint32_t kRankHighShift = 24;
  * uses the reference-format samples and counts. */
 constexpr uint32_t kDefaultSelShift = 7;
 
+/* rb_off / ds0_off of an array without rank blocks / dense samples (binary
+ * levels that quad levels cover); rank and select then use L1/L2. */
+constexpr uint64_t kNoBlocks = ~uint64_t(0);
+
 /* A set of bit arrays with rank/select support, all in device memory. */
 struct RSView {
   const uint32_t* words;
@@ -82,6 +86,40 @@ struct RSView {
   const uint32_t* ds;     // dense select samples (ArrayMeta::ds0/ds1_off)
   uint32_t num_arrays;
   uint32_t sel_shift;     // log2 of the dense sample rate; 0 = none
+};
+
+/* Quad (4-ary) query index of power-of-two alphabets (query side, no
+ * reference counterpart).  Quad level j pairs binary levels 2j and 2j+1: in
+ * level-2j order it holds each symbol's 2-bit digit (bit 2j as the high bit,
+ * bit 2j+1 as the low bit, counted from the top), so one read resolves two
+ * binary levels.  Storage: 32-byte blocks of 96 digits; bits 0..47 of a
+ * block hold the counts of digits 0, 1, 2 since the start of its superblock
+ * (512 blocks = 49,152 digits) as uint16, bits 64..255 the digits (digit t
+ * at bit 64 + 2t); a superblock table holds the four digit counts before
+ * every superblock (uint64).  Dense select samples per digit name the block
+ * holding every R-th occurrence (uint32).  node_ranks[j][g][d] = occurrences
+ * of digit d before node g of level 2j. */
+constexpr uint32_t kQuadDigits = 96;
+constexpr uint32_t kQuadSbBlocks = 512;
+constexpr uint64_t kQuadSbDigits = uint64_t(kQuadDigits) * kQuadSbBlocks;
+
+struct QuadLevel {
+  uint64_t blk_off;     // first block (2 uint4 each)
+  uint64_t sb_off;      // first superblock entry (4 uint64 each)
+  uint64_t ds_off[4];   // first dense sample of each digit
+  uint64_t total[4];    // occurrences of each digit
+  uint64_t nr_off;      // first node-rank entry (4 uint64 per node)
+  uint64_t num_blocks;  // n / 96 + 1 (position n is addressable)
+};
+
+struct QuadView {
+  const uint4* blocks;
+  const uint64_t* sb;
+  const uint32_t* ds;          // null: select searches the superblocks
+  const uint64_t* node_ranks;
+  const QuadLevel* levels;     // device array of num entries
+  uint32_t num;                // quad levels (0: the tree has none)
+  uint32_t sel_shift;          // log2 of the dense sample rate
 };
 
 /* Everything a query walk needs; trivially copyable into a kernel. */
@@ -103,6 +141,7 @@ struct TreeView {
   uint32_t elem_size;
   uint32_t is_pow2;
   uint32_t is_min;
+  QuadView quad;                   // quad levels over the binary ones
 };
 
 /* ---------------------------------------------------------------------- */
@@ -163,7 +202,7 @@ __device__ __forceinline__ uint64_t rs_rank1(const RSView& v,
     if (GetBit) *bit = false;
     return m.ones;
   }
-  if (v.rb) {
+  if (v.rb && m.rb_off != kNoBlocks) {
     // One 32-byte block: low word of the ones before it + 7 data words.
     uint64_t const blk = pos / kRankBlockBits;
     uint32_t const off = static_cast<uint32_t>(pos - blk * kRankBlockBits);
@@ -276,7 +315,8 @@ __device__ __forceinline__ uint64_t rs_select(const RSView& v,
                                               const ArrayMeta& m, uint64_t i) {
   uint64_t const total = Value ? m.ones : m.bits - m.ones;
   if (i == 0 || i > total) return m.bits;
-  if (v.sel_shift) return rs_select_dense<Value>(v, m, i, total);
+  if (v.sel_shift && m.ds0_off != kNoBlocks)
+    return rs_select_dense<Value>(v, m, i, total);
   uint64_t const* S = Value ? v.s1 + m.s1_off : v.s0 + m.s0_off;
   uint64_t const q = i / kSampleRate;
   uint64_t const lo = q ? __ldg(S + q - 1) : 0;
@@ -330,6 +370,161 @@ __device__ __forceinline__ uint64_t rs_select(const RSView& v,
   return m.bits;  // not reached for valid structures
 }
 
+/* ---- quad levels ------------------------------------------------------ */
+
+__device__ __forceinline__ void quad_words(uint4 a, uint4 b, uint64_t q[4]) {
+  q[0] = (uint64_t(a.y) << 32) | a.x;
+  q[1] = (uint64_t(a.w) << 32) | a.z;
+  q[2] = (uint64_t(b.y) << 32) | b.x;
+  q[3] = (uint64_t(b.w) << 32) | b.z;
+}
+
+/* Bit 2k of the result is set iff 2-bit lane k of q equals d. */
+__device__ __forceinline__ uint64_t quad_match(uint64_t q, uint32_t d) {
+  uint64_t const e = ~(q ^ (0x5555555555555555ull * d));
+  return e & (e >> 1) & 0x5555555555555555ull;
+}
+
+/* Digit-d count among the first t (<= 96) digits of a block (data words
+ * q[1..3], 32 digits each). */
+__device__ __forceinline__ uint32_t quad_count(uint64_t const q[4], uint32_t d,
+                                               uint32_t t) {
+  uint32_t c = 0;
+#pragma unroll
+  for (uint32_t w = 1; w < 4; ++w) {
+    uint32_t const lo = 32 * (w - 1);  // first digit of word w
+    uint64_t const mask = t >= lo + 32 ? ~0ull
+                          : t > lo     ? (1ull << (2 * (t - lo))) - 1
+                                       : 0ull;
+    c += __popcll(quad_match(q[w], d) & mask);
+  }
+  return c;
+}
+
+__device__ __forceinline__ uint32_t quad_digit(uint64_t const q[4], uint32_t t) {
+  uint64_t const w = t < 32 ? q[1] : t < 64 ? q[2] : q[3];
+  return static_cast<uint32_t>(w >> (2 * (t & 31))) & 3u;
+}
+
+/* Digit-d count before the block from its header and superblock entry. */
+__device__ __forceinline__ uint64_t quad_before(uint64_t q0, uint64_t sbv,
+                                                uint32_t d, uint64_t blk) {
+  uint32_t const h0 = static_cast<uint32_t>(q0) & 0xFFFFu;
+  uint32_t const h1 = static_cast<uint32_t>(q0 >> 16) & 0xFFFFu;
+  uint32_t const h2 = static_cast<uint32_t>(q0 >> 32) & 0xFFFFu;
+  uint32_t const in_sb = static_cast<uint32_t>(blk % kQuadSbBlocks) * kQuadDigits;
+  uint32_t const h = d == 0 ? h0 : d == 1 ? h1 : d == 2 ? h2 : in_sb - h0 - h1 - h2;
+  return sbv + h;
+}
+
+/* Digit at position p < n of quad level ql and its occurrences before p. */
+__device__ __forceinline__ uint32_t quad_access(const QuadView& v,
+                                                QuadLevel const& ql, uint64_t p,
+                                                uint64_t* before) {
+  uint64_t const blk = p / kQuadDigits;
+  uint32_t const t = static_cast<uint32_t>(p - blk * kQuadDigits);
+  uint4 const* bp = v.blocks + (ql.blk_off + blk) * 2;
+  uint4 const* sp = reinterpret_cast<uint4 const*>(
+      v.sb + (ql.sb_off + blk / kQuadSbBlocks) * 4);
+  uint4 const a = __ldg(bp), b = __ldg(bp + 1);
+  uint4 const s0 = __ldg(sp), s1 = __ldg(sp + 1);  // all four digit counts
+  uint64_t q[4];
+  quad_words(a, b, q);
+  uint32_t const d = quad_digit(q, t);
+  uint64_t const sbv = d == 0 ? ((uint64_t(s0.y) << 32) | s0.x)
+                       : d == 1 ? ((uint64_t(s0.w) << 32) | s0.z)
+                       : d == 2 ? ((uint64_t(s1.y) << 32) | s1.x)
+                                : ((uint64_t(s1.w) << 32) | s1.z);
+  *before = quad_before(q[0], sbv, d, blk) + quad_count(q, d, t);
+  return d;
+}
+
+/* Occurrences of digit d in [0, p) of quad level ql, p <= n. */
+__device__ __forceinline__ uint64_t quad_rank(const QuadView& v,
+                                              QuadLevel const& ql, uint64_t p,
+                                              uint32_t d) {
+  uint64_t const blk = p / kQuadDigits;
+  uint32_t const t = static_cast<uint32_t>(p - blk * kQuadDigits);
+  uint4 const* bp = v.blocks + (ql.blk_off + blk) * 2;
+  uint4 const a = __ldg(bp), b = __ldg(bp + 1);
+  uint64_t const sbv = __ldg(v.sb + (ql.sb_off + blk / kQuadSbBlocks) * 4 + d);
+  uint64_t q[4];
+  quad_words(a, b, q);
+  return quad_before(q[0], sbv, d, blk) + quad_count(q, d, t);
+}
+
+/* Position of the k-th (1-based, k <= total[d]) digit d of quad level ql:
+ * dense samples bracket its block (without them the superblock table does),
+ * a binary search over block counts narrows wide brackets to two blocks,
+ * both read at once, then the in-block scan. */
+__device__ __forceinline__ uint64_t quad_select(const QuadView& v,
+                                                QuadLevel const& ql,
+                                                uint32_t d, uint64_t k) {
+  uint64_t const nblk = ql.num_blocks;
+  if (k == 0 || k > ql.total[d]) return nblk * kQuadDigits;  // invalid structure
+  uint64_t const* sb = v.sb + ql.sb_off * 4 + d;
+  uint4 const* blocks = v.blocks + ql.blk_off * 2;
+  uint64_t lo, hi;
+  if (v.ds) {
+    uint32_t const sh = v.sel_shift;
+    uint32_t const* S = v.ds + ql.ds_off[d];
+    uint64_t const j = (k - 1) >> sh;
+    lo = min(uint64_t(__ldg(S + j)), nblk - 1);
+    hi = ((j + 1) << sh) < ql.total[d] ? __ldg(S + j + 1) : nblk - 1;
+    hi = min(max(hi, lo), nblk - 1);
+  } else {  // superblock whose count before it is below k
+    uint64_t a = 0, z = (nblk - 1) / kQuadSbBlocks;
+    while (a < z) {
+      uint64_t const mid = (a + z + 1) >> 1;
+      if (__ldg(sb + mid * 4) < k) a = mid; else z = mid - 1;
+    }
+    lo = a * kQuadSbBlocks;
+    hi = min(lo + kQuadSbBlocks - 1, nblk - 1);
+  }
+  auto before = [&](uint64_t blk) -> uint64_t {
+    uint4 const h = __ldg(blocks + blk * 2);
+    return quad_before((uint64_t(h.y) << 32) | h.x,
+                       __ldg(sb + (blk / kQuadSbBlocks) * 4), d, blk);
+  };
+  while (hi - lo > 1) {
+    uint64_t const mid = (lo + hi + 1) >> 1;
+    if (before(mid) < k) lo = mid; else hi = mid - 1;
+  }
+  uint4 const a0 = __ldg(blocks + lo * 2), a1 = __ldg(blocks + lo * 2 + 1);
+  uint4 const c0 = __ldg(blocks + hi * 2), c1 = __ldg(blocks + hi * 2 + 1);
+  uint64_t qa[4], qc[4];
+  quad_words(a0, a1, qa);
+  quad_words(c0, c1, qc);
+  uint64_t const bh = quad_before(qc[0], __ldg(sb + (hi / kQuadSbBlocks) * 4), d, hi);
+  bool const in_hi = hi > lo && bh < k;
+  uint64_t const blk = in_hi ? hi : lo;
+  uint64_t const bt =
+      in_hi ? bh : quad_before(qa[0], __ldg(sb + (lo / kQuadSbBlocks) * 4), d, lo);
+  uint32_t r = static_cast<uint32_t>(k - bt);  // 1 ..= 96
+  uint32_t pos = 0;
+  bool found = false;
+#pragma unroll
+  for (uint32_t w = 1; w < 4; ++w) {
+    uint64_t const m = quad_match(in_hi ? qc[w] : qa[w], d);
+    uint32_t const c = __popcll(m);
+    if (!found) {
+      if (r <= c) {
+        uint32_t const lo32 = static_cast<uint32_t>(m);
+        uint32_t const cl = __popc(lo32);
+        uint32_t const bit = r <= cl
+                                 ? select_in_word(lo32, r)
+                                 : 32 + select_in_word(static_cast<uint32_t>(m >> 32), r - cl);
+        pos = 32 * (w - 1) + bit / 2;
+        found = true;
+      } else {
+        r -= c;
+      }
+    }
+  }
+  if (!found) return nblk * kQuadDigits;  // not reached for valid structures
+  return blk * kQuadDigits + pos;
+}
+
 /* ---- tree walks ------------------------------------------------------- */
 
 /* Index into node_ranks of the node starting at symbol cs on level l >= 1
@@ -364,6 +559,93 @@ __device__ __forceinline__ uint64_t occurrences(const TreeView& t,
   return (c + 1 == t.sigma ? t.n : counts[c + 1]) - counts[c];
 }
 
+/* The three walks over quad levels (power-of-two alphabets): the same
+ * descent as the binary walks below, two binary levels per step; an odd
+ * last binary level is walked as in the binary code. */
+__device__ __forceinline__ uint64_t quad_node_rank(const TreeView& t,
+                                                   QuadLevel const& ql,
+                                                   uint64_t g, uint32_t d) {
+  return __ldg(t.quad.node_ranks + ql.nr_off + g * 4 + d);
+}
+
+__device__ __forceinline__ uint64_t wt_access_quad(const TreeView& t,
+                                                   ArrayMeta const* meta,
+                                                   uint64_t const* counts,
+                                                   uint64_t idx) {
+  uint32_t const L = t.levels;
+  uint64_t cs = 0;
+  for (uint32_t j = 0; j < t.quad.num; ++j) {
+    QuadLevel const& ql = t.quad.levels[j];
+    uint32_t const sh = L - 2 * j;  // log2 of the symbols under a level-2j node
+    uint64_t before;
+    uint32_t const d = quad_access(t.quad, ql, counts[cs] + idx, &before);
+    if (j + 1 < t.quad.num || (L & 1))
+      idx = before - quad_node_rank(t, ql, cs >> sh, d);
+    cs += uint64_t(d) << (sh - 2);
+  }
+  if (L & 1) {  // last binary level: its bit alone
+    if (rs_bit(t.rs, meta[L - 1], counts[cs] + idx)) cs += 1;
+  }
+  return cs;
+}
+
+__device__ __forceinline__ uint64_t wt_rank_quad(const TreeView& t,
+                                                 ArrayMeta const* meta,
+                                                 uint64_t const* counts,
+                                                 uint64_t const* ranks,
+                                                 uint64_t const* node_base,
+                                                 uint64_t c, uint64_t i) {
+  uint32_t const L = t.levels;
+  uint64_t cs = 0, res = i;
+  for (uint32_t j = 0; j < t.quad.num; ++j) {
+    QuadLevel const& ql = t.quad.levels[j];
+    uint32_t const sh = L - 2 * j;
+    uint32_t const d = static_cast<uint32_t>(c >> (sh - 2)) & 3u;
+    res = quad_rank(t.quad, ql, counts[cs] + res, d) -
+          quad_node_rank(t, ql, cs >> sh, d);
+    cs += uint64_t(d) << (sh - 2);
+  }
+  if (L & 1) {
+    ArrayMeta const& m = meta[L - 1];
+    uint64_t const start = cs ? ranks[node_index(t, node_base, cs, L - 1)] : 0;
+    uint64_t const p = counts[cs] + res;
+    uint64_t const r0 = p - rs_rank1<false>(t.rs, m, p, nullptr);
+    if (c & 1) res -= r0 - start; else res = r0 - start;
+  }
+  return res;
+}
+
+__device__ __forceinline__ uint64_t wt_select_quad(const TreeView& t,
+                                                   ArrayMeta const* meta,
+                                                   uint64_t const* counts,
+                                                   uint64_t const* ranks,
+                                                   uint64_t const* node_base,
+                                                   uint64_t c, uint64_t k) {
+  uint32_t const L = t.levels;
+  uint64_t res = k;  // 1-based occurrence inside the current node
+  if (L & 1) {
+    ArrayMeta const& m = meta[L - 1];
+    uint64_t const cs = c & ~uint64_t(1);
+    uint64_t const z = cs ? ranks[node_index(t, node_base, cs, L - 1)] : 0;
+    if (c & 1)
+      res = rs_select<1>(t.rs, m, (cs ? counts[cs] - z : 0) + res) + 1;
+    else
+      res = rs_select<0>(t.rs, m, z + res) + 1;
+    if (res > m.bits) return t.n;
+    res -= counts[cs];
+  }
+  for (int j = int(t.quad.num) - 1; j >= 0; --j) {
+    QuadLevel const& ql = t.quad.levels[j];
+    uint32_t const sh = L - 2 * uint32_t(j);
+    uint64_t const g = c >> sh;
+    uint32_t const d = static_cast<uint32_t>(c >> (sh - 2)) & 3u;
+    uint64_t const pos =
+        quad_select(t.quad, ql, d, quad_node_rank(t, ql, g, d) + res);
+    res = pos + 1 - counts[g << sh];
+  }
+  return res - 1;
+}
+
 /* Minimal symbol at text position idx < n (deviceAccess,
  * wavelet_tree.cuh:1815-1877). */
 __device__ __forceinline__ uint64_t wt_access(const TreeView& t,
@@ -372,6 +654,7 @@ __device__ __forceinline__ uint64_t wt_access(const TreeView& t,
                                               uint64_t const* ranks,
                                               uint64_t const* node_base,
                                               uint64_t idx) {
+  if (t.quad.num) return wt_access_quad(t, meta, counts, idx);
   uint64_t cs = 0, ce = t.sigma - 1;
   for (uint32_t l = 0; l < t.levels; ++l) {
     ArrayMeta const& m = meta[l];
@@ -405,6 +688,7 @@ __device__ __forceinline__ uint64_t wt_rank(const TreeView& t,
                                             uint64_t const* node_base,
                                             uint64_t c, uint64_t i) {
   if (occurrences(t, counts, c) == 0) return 0;
+  if (t.quad.num) return wt_rank_quad(t, meta, counts, ranks, node_base, c, i);
   uint64_t cs = 0, ce = t.sigma - 1, res = i;
   for (uint32_t l = 0; l < t.levels; ++l) {
     if (ce == cs) break;
@@ -435,6 +719,7 @@ __device__ __forceinline__ uint64_t wt_select(const TreeView& t,
                                               uint64_t const* node_base,
                                               uint64_t c, uint64_t k) {
   if (k == 0 || k > occurrences(t, counts, c)) return t.n;
+  if (t.quad.num) return wt_select_quad(t, meta, counts, ranks, node_base, c, k);
   uint32_t const L = t.levels;
   uint64_t len = L, code = c;
   if (!t.is_pow2 && c >= t.codes_start) {

@@ -200,7 +200,8 @@ int ewt_rs_get_device_view(const ewt_rs* rs, void* view_out,
 #define EWT_PHASE_SAMPLES 5    /* select samples                           */
 #define EWT_PHASE_QUERY 6      /* query kernels                            */
 #define EWT_PHASE_H2D 7        /* host-to-device text copy                 */
-#define EWT_NUM_PHASES 8
+#define EWT_PHASE_QUAD 8       /* quad query levels                        */
+#define EWT_NUM_PHASES 9
 typedef struct ewt_phase_times {
   double ms[EWT_NUM_PHASES];        /* accumulated device milliseconds    */
   uint64_t launches[EWT_NUM_PHASES]; /* timed launches per phase          */
