@@ -243,10 +243,12 @@ __device__ __forceinline__ void put_quad_samples(uint32_t* __restrict__ ds,
 #pragma unroll
   for (uint32_t d = 0; d < 4; ++d) {
     if (c[d] == 0) continue;
-    uint64_t const entries = (ql.total[d] + R - 1) >> sh;
-    uint64_t const last = min((before[d] + c[d] - 1) >> sh, entries - 1);
+    // entries fit in 32 bits (at most n / 32 of them)
+    uint32_t const entries = static_cast<uint32_t>((ql.total[d] + R - 1) >> sh);
+    uint32_t const last =
+        min(static_cast<uint32_t>((before[d] + c[d] - 1) >> sh), entries - 1);
     uint32_t* S = ds + ql.ds_off[d];
-    for (uint64_t k = (before[d] + R - 1) >> sh; k <= last; ++k)
+    for (uint32_t k = static_cast<uint32_t>((before[d] + R - 1) >> sh); k <= last; ++k)
       S[k] = static_cast<uint32_t>(blk);
   }
 }
@@ -320,6 +322,34 @@ __device__ __forceinline__ uint64_t half_exclusive_scan(uint64_t x, uint64_t* to
   return before + inc - x;
 }
 
+// half_exclusive_scan for 32-bit values.
+__device__ __forceinline__ uint32_t half_exclusive_scan32(uint32_t x, uint32_t* total) {
+  __shared__ uint32_t ws32[32];
+  uint32_t const lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t inc = x;
+#pragma unroll
+  for (uint32_t o = 1; o < 32; o <<= 1) {
+    uint32_t const y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) ws32[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t t = ws32[lane];
+#pragma unroll
+    for (uint32_t o = 1; o < 16; o <<= 1) {
+      uint32_t const y = __shfl_up_sync(0xFFFFFFFFu, t, o);
+      if ((lane & 15) >= o) t += y;
+    }
+    ws32[lane] = t;
+  }
+  __syncthreads();
+  uint32_t const before = (wid & 15) ? ws32[wid - 1] : 0;
+  *total = ws32[(wid & 16) + 15];
+  __syncthreads();
+  return before + inc - x;
+}
+
 // Pass 3: persistent CTAs of 1024 threads, two superblocks at a time (one
 // per 512-thread half, one thread per 96-digit block), the digit table in
 // shared memory.
@@ -351,20 +381,22 @@ quad_level_kernel(TreeView v, uint32_t j, QuadLevel ql,
     bool const mine = live && blk < ql.num_blocks;
     uint64_t const p = blk * kQuadDigits;
     uint32_t h[3], vm[3];
-    uint32_t ones = 0, valid_all = 0;
+    uint32_t ones = 0;
 #pragma unroll
     for (uint32_t k = 0; k < 3; ++k) {
       uint64_t const w = blk * 3 + k;
       uint64_t const p0 = p + 32 * k;
       uint32_t const valid =
           mine && p0 < n ? static_cast<uint32_t>(min(uint64_t(32), n - p0)) : 0u;
-      valid_all += valid;
       vm[k] = valid == 32 ? ~0u : (1u << valid) - 1u;
       h[k] = valid && w < hi_words ? hi_w[w] & vm[k] : 0u;
       ones += __popc(h[k]);
     }
-    uint64_t tot = 0;
-    uint64_t r1 = st.rank1 + half_exclusive_scan(ones, &tot);  // ones before p
+    uint32_t tot = 0;
+    // ones of level 2j in the superblock before this block (= its digits 2
+    // and 3 before it)
+    uint32_t const h23 = half_exclusive_scan32(ones, &tot);
+    uint64_t r1 = st.rank1 + h23;  // ones before p
     uint32_t dw[6] = {0, 0, 0, 0, 0, 0};
     uint64_t const right = st.node.start + st.node.zeros;  // right child start
 #pragma unroll
@@ -408,40 +440,36 @@ quad_level_kernel(TreeView v, uint32_t j, QuadLevel ql,
       }
       r1 += __popc(h[k]);
     }
-    uint32_t c[4] = {0, 0, 0, 0};
+    uint32_t c1 = 0, c3 = 0;  // digits 1 and 3 of the block
 #pragma unroll
     for (uint32_t k = 0; k < 6; ++k) {
       uint32_t const lo = dw[k] & 0x55555555u, hi = (dw[k] >> 1) & 0x55555555u;
-      c[3] += __popc(lo & hi);
-      c[2] += __popc(hi & ~lo);
-      c[1] += __popc(lo & ~hi);
+      c3 += __popc(lo & hi);
+      c1 += __popc(lo & ~hi);
     }
-    c[0] = valid_all - c[1] - c[2] - c[3];
-    // counts of digits 0..2 packed 21 bits apart (each below 2^16): one scan
-    uint64_t const packed = uint64_t(c[0]) | (uint64_t(c[1]) << 21) | (uint64_t(c[2]) << 42);
-    uint64_t const hd = half_exclusive_scan(packed, &tot);
+    uint32_t tot13 = 0;
+    uint32_t const h13 = half_exclusive_scan32(c1 | (c3 << 16), &tot13);  // each < 2^16
     if (!live) continue;
     uint64_t const* sbe = sb + sbi * 4;
+    uint32_t const in_sb = t * kQuadDigits;  // positions before the block
+    uint32_t const h1 = h13 & 0xFFFFu, h3 = h13 >> 16;
+    uint32_t const h0 = in_sb - h23 - h1, h2 = h23 - h3;
     if (t == 0) {  // the pass-1 counts must agree
       uint64_t const first = sbi * kQuadSbDigits;
-      uint64_t const in_sb = first < n ? min(kQuadSbDigits, n - first) : 0;
-      uint64_t const t0 = tot & 0x1FFFFFu, t1 = (tot >> 21) & 0x1FFFFFu,
-                     t2 = (tot >> 42) & 0x1FFFFFu;
-      if (sbe[4] - sbe[0] != t0 || sbe[5] - sbe[1] != t1 || sbe[6] - sbe[2] != t2 ||
-          sbe[7] - sbe[3] != in_sb - t0 - t1 - t2)
+      uint32_t const all = first < n ? static_cast<uint32_t>(min(kQuadSbDigits, n - first)) : 0u;
+      uint32_t const t1 = tot13 & 0xFFFFu, t3 = tot13 >> 16;
+      if (sbe[5] - sbe[1] != t1 || sbe[7] - sbe[3] != t3 ||
+          sbe[6] - sbe[2] != tot - t3 || sbe[4] - sbe[0] != all - tot - t1)
         atomicOr(err, 2u);
     }
     if (!mine) continue;
-    uint32_t const h0 = static_cast<uint32_t>(hd & 0x1FFFFFu);
-    uint32_t const h1 = static_cast<uint32_t>((hd >> 21) & 0x1FFFFFu);
-    uint32_t const h2 = static_cast<uint32_t>((hd >> 42) & 0x1FFFFFu);
     uint4* out = blocks + blk * 2;
     out[0] = make_uint4(h0 | (h1 << 16), h2, dw[0], dw[1]);
     out[1] = make_uint4(dw[2], dw[3], dw[4], dw[5]);
     if (ds) {
-      uint32_t const in_sb = t * kQuadDigits;
-      uint64_t const before[4] = {sbe[0] + h0, sbe[1] + h1, sbe[2] + h2,
-                                  sbe[3] + (in_sb - h0 - h1 - h2)};
+      uint32_t const vb = static_cast<uint32_t>(min(uint64_t(kQuadDigits), n - p));
+      uint32_t const c[4] = {vb - ones - c1, c1, ones - c3, c3};
+      uint64_t const before[4] = {sbe[0] + h0, sbe[1] + h1, sbe[2] + h2, sbe[3] + h3};
       put_quad_samples(ds, ql, sel_shift, blk, before, c);
     }
   }
