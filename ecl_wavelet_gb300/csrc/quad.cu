@@ -209,26 +209,35 @@ __global__ void quad_scan_chunks_kernel(uint64_t* __restrict__ chunk,
   }
 }
 
-// Pass 2c: exclusive prefix of every entry, in place.
-__global__ void __launch_bounds__(256)
+// Pass 2c: exclusive prefix of every entry, in place (1024 threads; two
+// digits packed per 64-bit scan: a round's sums stay below 2^32).
+__global__ void __launch_bounds__(1024)
 quad_scan_apply_kernel(uint64_t* __restrict__ sb, uint64_t count,
                        uint64_t const* __restrict__ chunk) {
   uint64_t const first = uint64_t(blockIdx.x) * kScanChunk;
+  uint64_t const end = min(count, first + kScanChunk);
   uint64_t carry[4];
-  for (uint32_t d = 0; d < 4; ++d) carry[d] = chunk[blockIdx.x * 4 + d];
-  for (uint64_t base = first; base < min(count, first + kScanChunk);
-       base += blockDim.x) {
+  for (uint32_t d = 0; d < 4; ++d) carry[d] = chunk ? chunk[blockIdx.x * 4 + d] : 0;
+  for (uint64_t base = first; base < end; base += blockDim.x) {
     uint64_t const i = base + threadIdx.x;
-    bool const in = i < min(count, first + kScanChunk);
-    uint64_t x[4] = {0, 0, 0, 0};
-    if (in)
-      for (uint32_t d = 0; d < 4; ++d) x[d] = sb[i * 4 + d];
-    for (uint32_t d = 0; d < 4; ++d) {
-      uint64_t tot = 0;
-      uint64_t const ex = cta_exclusive_scan(x[d], &tot);
-      if (in) sb[i * 4 + d] = carry[d] + ex;
-      carry[d] += tot;
+    bool const in = i < end;
+    uint4 const a = in ? reinterpret_cast<uint4 const*>(sb)[i * 2] : make_uint4(0, 0, 0, 0);
+    uint4 const b = in ? reinterpret_cast<uint4 const*>(sb)[i * 2 + 1] : make_uint4(0, 0, 0, 0);
+    // per entry each digit count is below 2^16 (49,152 digits per superblock)
+    uint64_t tot01 = 0, tot23 = 0;
+    uint64_t const e01 = cta_exclusive_scan(uint64_t(a.x) | (uint64_t(a.z) << 32), &tot01);
+    uint64_t const e23 = cta_exclusive_scan(uint64_t(b.x) | (uint64_t(b.z) << 32), &tot23);
+    if (in) {
+      uint64_t* o = sb + i * 4;
+      o[0] = carry[0] + (e01 & 0xFFFFFFFFu);
+      o[1] = carry[1] + (e01 >> 32);
+      o[2] = carry[2] + (e23 & 0xFFFFFFFFu);
+      o[3] = carry[3] + (e23 >> 32);
     }
+    carry[0] += tot01 & 0xFFFFFFFFu;
+    carry[1] += tot01 >> 32;
+    carry[2] += tot23 & 0xFFFFFFFFu;
+    carry[3] += tot23 >> 32;
   }
 }
 
@@ -621,13 +630,15 @@ void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, cudaStream_t st) {
         v, j, nsb, sb, info.as<SbStart>());
     EWT_LAUNCHED();
     uint64_t const chunks = ceil_div(nsb + 1, kScanChunk);
-    quad_scan_partial_kernel<<<static_cast<uint32_t>(chunks), 256, 0, st>>>(
-        sb, nsb + 1, chunk.as<uint64_t>());
-    EWT_LAUNCHED();
-    quad_scan_chunks_kernel<<<1, 32, 0, st>>>(chunk.as<uint64_t>(), chunks);
-    EWT_LAUNCHED();
-    quad_scan_apply_kernel<<<static_cast<uint32_t>(chunks), 256, 0, st>>>(
-        sb, nsb + 1, chunk.as<uint64_t>());
+    if (chunks > 1) {
+      quad_scan_partial_kernel<<<static_cast<uint32_t>(chunks), 256, 0, st>>>(
+          sb, nsb + 1, chunk.as<uint64_t>());
+      EWT_LAUNCHED();
+      quad_scan_chunks_kernel<<<1, 32, 0, st>>>(chunk.as<uint64_t>(), chunks);
+      EWT_LAUNCHED();
+    }
+    quad_scan_apply_kernel<<<static_cast<uint32_t>(chunks), 1024, 0, st>>>(
+        sb, nsb + 1, chunks > 1 ? chunk.as<uint64_t>() : nullptr);
     EWT_LAUNCHED();
     uint32_t const grid = static_cast<uint32_t>(
         std::min<uint64_t>(ceil_div(nsb, 2), uint64_t(sm_count())));
