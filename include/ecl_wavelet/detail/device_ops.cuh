@@ -67,7 +67,7 @@ constexpr uint32_t kRankHighShift = 24;
  * select reads two neighbouring entries, which bracket its block, and then
  * one or two rank blocks; sel_shift = 0 means none were built and select
  * uses the reference-format samples and counts. */
-constexpr uint32_t kDefaultSelShift = 7;
+constexpr uint32_t kDefaultSelShift = 6;
 
 /* rb_off / ds0_off of an array without rank blocks / dense samples (binary
  * levels that quad levels cover); rank and select then use L1/L2. */
@@ -486,26 +486,34 @@ __device__ __forceinline__ uint64_t quad_select(const QuadView& v,
     return quad_before((uint64_t(h.y) << 32) | h.x,
                        __ldg(sb + (blk / kQuadSbBlocks) * 4), d, blk);
   };
-  while (hi - lo > 1) {
+  while (hi - lo > 2) {  // wide brackets only (rare digits)
     uint64_t const mid = (lo + hi + 1) >> 1;
     if (before(mid) < k) lo = mid; else hi = mid - 1;
   }
+  // up to three blocks read at once; the last whose count before it is
+  // below k holds the k-th digit
+  uint64_t const mb = min(lo + 1, hi);
   uint4 const a0 = __ldg(blocks + lo * 2), a1 = __ldg(blocks + lo * 2 + 1);
+  uint4 const b0 = __ldg(blocks + mb * 2), b1 = __ldg(blocks + mb * 2 + 1);
   uint4 const c0 = __ldg(blocks + hi * 2), c1 = __ldg(blocks + hi * 2 + 1);
-  uint64_t qa[4], qc[4];
+  uint64_t const sa = __ldg(sb + (lo / kQuadSbBlocks) * 4);
+  uint64_t const sm = __ldg(sb + (mb / kQuadSbBlocks) * 4);
+  uint64_t const sc = __ldg(sb + (hi / kQuadSbBlocks) * 4);
+  uint64_t qa[4], qb[4], qc[4];
   quad_words(a0, a1, qa);
+  quad_words(b0, b1, qb);
   quad_words(c0, c1, qc);
-  uint64_t const bh = quad_before(qc[0], __ldg(sb + (hi / kQuadSbBlocks) * 4), d, hi);
-  bool const in_hi = hi > lo && bh < k;
-  uint64_t const blk = in_hi ? hi : lo;
-  uint64_t const bt =
-      in_hi ? bh : quad_before(qa[0], __ldg(sb + (lo / kQuadSbBlocks) * 4), d, lo);
+  uint64_t const bm = quad_before(qb[0], sm, d, mb);
+  uint64_t const bh = quad_before(qc[0], sc, d, hi);
+  int const which = (hi > mb && bh < k) ? 2 : (mb > lo && bm < k) ? 1 : 0;
+  uint64_t const blk = which == 2 ? hi : which == 1 ? mb : lo;
+  uint64_t const bt = which == 2 ? bh : which == 1 ? bm : quad_before(qa[0], sa, d, lo);
   uint32_t r = static_cast<uint32_t>(k - bt);  // 1 ..= 96
   uint32_t pos = 0;
   bool found = false;
 #pragma unroll
   for (uint32_t w = 1; w < 4; ++w) {
-    uint64_t const m = quad_match(in_hi ? qc[w] : qa[w], d);
+    uint64_t const m = quad_match(which == 2 ? qc[w] : which == 1 ? qb[w] : qa[w], d);
     uint32_t const c = __popcll(m);
     if (!found) {
       if (r <= c) {

@@ -220,7 +220,7 @@ uint64_t ewt_launch_count(void);
  * Times the query kernels on probe_queries device-generated valid queries
  * over this tree and keeps the fastest configuration for every later query
  * on it: first the dense select-sample rate (every R-th zero / one, R in
- * {64, 128, 256, 512}, or none: the reference-format samples alone), timed
+ * {32, 64, 128, 256, 512}, or none: the reference-format samples alone), timed
  * on select probes, then per kind (access, rank, select, mixed) the launch
  * shape (threads per CTA x resident CTAs per SM).  *out (may be NULL)
  * reports the choices and the default and tuned rates.  Results never
@@ -240,8 +240,9 @@ int ewt_autotune(ewt_tree* tree, uint64_t probe_queries, ewt_tuning* out);
 
 /* Rebuilds the dense select samples (query side, beside the reference-format
  * samples, which exports keep) at one entry per `rate` zeros / ones: 0 drops
- * them (select then runs the reference's sample -> L1 -> L2 search), else a
- * power of two in [32, 65536]; each entry costs 4 bytes.  Built at 128 by
+ * them (select then runs the reference's sample -> L1 -> L2 search, or on
+ * quad levels a search of the superblock table), else a
+ * power of two in [32, 65536]; each entry costs 4 bytes.  Built at 64 by
  * default.  Refused (EWT_ERR_INVALID_ARGUMENT) once the device view was
  * copied out.  No reference counterpart (rank_select.cuh:44-64 fixes one
  * sample per 4096 at compile time). */
