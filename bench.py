@@ -788,10 +788,11 @@ def run_ours(args, world, rank, local):
     h_np = h_text.numpy()
     tree.close()
     tree = None
-    E.WaveletTree(h_np, alphabet, gpu_index=local).close()
+    for _ in range(max(args.warmup, 3)):  # warm-up: pool and page tables
+        E.WaveletTree(h_np, alphabet, gpu_index=local).close()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    reps = 2
+    reps = 3
     for _ in range(reps):
         tr = E.WaveletTree(h_np, alphabet, gpu_index=local)
         ones = tr.export("TOTAL_ONES")  # result read back to the host
