@@ -118,6 +118,8 @@ void populate_for_write(void* p, size_t bytes) {
 
 // Largest batch moved through the device scratch in one piece.
 constexpr uint64_t kChunk = uint64_t(1) << 25;
+// Host batches from this size on run pipelined (QueryPipe).
+constexpr uint64_t kPipeMin = uint64_t(1) << 21;
 
 void ensure(DevBuf& b, size_t& cap, size_t bytes) {
   if (bytes <= cap && b.get()) return;
@@ -187,6 +189,48 @@ int host_batch(ewt_tree* t, void const* in, size_t in_rec, uint8_t const* types,
     DeviceGuard g(t->device);
     AllocStream as(t->stream);
     cudaStream_t s = t->stream;
+    if (m >= kPipeMin) {
+      // large batches: copies in and out overlap the kernels chunk by chunk
+      // (copy engines reach the C2C bandwidth; the kernel then works on
+      // device memory only)
+      populate_for_write(out, m * out_rec);
+      QueryPipe& P = t->pipe;
+      P.init();
+      uint64_t const chunk = std::max<uint64_t>(kPipeMin / 4, ceil_div(m, 8));
+      for (int x = 0; x < 2; ++x) {  // allocated on s, before the copy streams start
+        ensure(P.in[x], P.cap_in[x], chunk * in_rec);
+        ensure(P.out[x], P.cap_out[x], chunk * out_rec);
+        if (types) ensure(P.types[x], P.cap_types[x], chunk);
+      }
+      EWT_CUDA(cudaEventRecord(P.start, s));
+      EWT_CUDA(cudaStreamWaitEvent(P.s_in, P.start, 0));
+      uint64_t i = 0;
+      for (uint64_t b = 0; b < m; b += chunk, ++i) {
+        int const x = static_cast<int>(i & 1);
+        uint64_t const k = std::min(chunk, m - b);
+        if (i >= 2) EWT_CUDA(cudaStreamWaitEvent(P.s_in, P.k_done[x], 0));
+        EWT_CUDA(cudaMemcpyAsync(P.in[x].get(), static_cast<char const*>(in) + b * in_rec,
+                                 k * in_rec, cudaMemcpyDefault, P.s_in));
+        if (types)
+          EWT_CUDA(cudaMemcpyAsync(P.types[x].get(), types + b, k, cudaMemcpyDefault,
+                                   P.s_in));
+        EWT_CUDA(cudaEventRecord(P.in_done[x], P.s_in));
+        EWT_CUDA(cudaStreamWaitEvent(s, P.in_done[x], 0));
+        if (i >= 2) EWT_CUDA(cudaStreamWaitEvent(s, P.out_done[x], 0));
+        launch(P.types[x].as<uint8_t>(), P.in[x].get(), k, P.out[x].get(), s);
+        EWT_CUDA(cudaEventRecord(P.k_done[x], s));
+        EWT_CUDA(cudaStreamWaitEvent(P.s_out, P.k_done[x], 0));
+        EWT_CUDA(cudaMemcpyAsync(static_cast<char*>(out) + b * out_rec, P.out[x].get(),
+                                 k * out_rec, cudaMemcpyDefault, P.s_out));
+        EWT_CUDA(cudaEventRecord(P.out_done[x], P.s_out));
+      }
+      EWT_CUDA(cudaStreamWaitEvent(s, P.out_done[(i - 1) & 1], 0));
+      int const st = take_query_status(t->err_d, s);
+      if (st != EWT_OK)
+        throw Error(st, "the batch held invalid queries (their results are "
+                        "UINT64_MAX)");
+      return;
+    }
     if (pageable_access(t->device)) {
       // the kernel reads the caller's queries and writes its results in
       // place (host page tables): no staging copies

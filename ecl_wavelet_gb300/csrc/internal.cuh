@@ -74,6 +74,37 @@ struct QueryScratch {
   size_t in_cap = 0, out_cap = 0, types_cap = 0;
 };
 
+// Streams, events and double buffers of pipelined host batches: queries of
+// chunk i+1 copied in and results of chunk i-1 copied out while chunk i is
+// answered (capi.cu).  Created on first use.
+struct QueryPipe {
+  cudaStream_t s_in = nullptr, s_out = nullptr;
+  cudaEvent_t start = nullptr, in_done[2] = {}, k_done[2] = {}, out_done[2] = {};
+  DevBuf in[2], out[2], types[2];
+  size_t cap_in[2] = {0, 0}, cap_out[2] = {0, 0}, cap_types[2] = {0, 0};
+  void init() {
+    if (s_in) return;
+    EWT_CUDA(cudaStreamCreateWithFlags(&s_in, cudaStreamNonBlocking));
+    EWT_CUDA(cudaStreamCreateWithFlags(&s_out, cudaStreamNonBlocking));
+    EWT_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+    for (int i = 0; i < 2; ++i) {
+      EWT_CUDA(cudaEventCreateWithFlags(&in_done[i], cudaEventDisableTiming));
+      EWT_CUDA(cudaEventCreateWithFlags(&k_done[i], cudaEventDisableTiming));
+      EWT_CUDA(cudaEventCreateWithFlags(&out_done[i], cudaEventDisableTiming));
+    }
+  }
+  ~QueryPipe() {
+    if (!s_in) return;
+    cudaStreamSynchronize(s_in);
+    cudaStreamSynchronize(s_out);
+    for (cudaEvent_t e : {start, in_done[0], in_done[1], k_done[0], k_done[1],
+                          out_done[0], out_done[1]})
+      if (e) cudaEventDestroy(e);
+    cudaStreamDestroy(s_in);
+    cudaStreamDestroy(s_out);
+  }
+};
+
 struct CodeH {
   uint64_t len, code;
 };
@@ -111,6 +142,7 @@ struct ewt_tree {
   ecl::detail::TreeView view{};
   std::mutex query_mu;  // host batch calls share scratch buffers
   ewt::QueryScratch scratch;
+  ewt::QueryPipe pipe;
   cudaStream_t stream = nullptr;  // library-owned stream for host calls
   uint64_t device_bytes() const;
 };

@@ -317,3 +317,28 @@ def test_large_text_round_trips(ewt, n, sigma):
     assert np.array_equal(t.select(t.make_queries(r + 1, c)), idx)
     assert np.array_equal(t.rank(t.make_queries(np.full(sigma, n), np.arange(sigma))),
                           occ.astype(np.uint64))
+
+
+@pytest.mark.parametrize("dtype,sigma", [(np.uint8, 256), (np.uint16, 1000)])
+def test_pipelined_host_batches(ewt, oracle, dtype, sigma):
+    """Host batches of 2^21 queries and more run pipelined (queries copied
+    in and results copied out chunk by chunk while other chunks are
+    answered); every answer equals the oracle's walk, including a ragged
+    last chunk."""
+    from tests.workloads import random_queries, random_text
+    rng = np.random.default_rng(sigma)
+    text, alphabet = random_text(rng, 1 << 22, sigma, dtype, minimal=sigma == 256)
+    gt = ewt.WaveletTree(text, alphabet)
+    ot = oracle.OracleTree(text, alphabet)
+    m = (1 << 21) + 4097
+    idx, rk, rs, sk, ss = random_queries(rng, text, np.asarray(alphabet, np.uint64), m)
+    assert np.array_equal(gt.access(idx).astype(np.uint64), ot.access(idx))
+    want, st = ot.rank(rk, rs)
+    assert st == 0
+    assert np.array_equal(gt.rank(gt.make_queries(rk, rs)), want)
+    types = rng.integers(0, 3, m).astype(np.uint8)
+    index = np.where(types == 0, idx, np.where(types == 1, rk, sk))
+    sym = np.where(types == 1, rs, ss)
+    want, st = ot.mixed(types, index, sym)
+    assert st == 0
+    assert np.array_equal(gt.mixed(types, gt.make_queries(index, sym)), want)
