@@ -302,66 +302,41 @@ __device__ __forceinline__ void digits_fast(uint16_t const* lut, uint32_t h,
   dhi = d[2] | (d[3] << 16);
 }
 
-// Exclusive scan over the threads of one 512-thread half of a 1024-thread
-// CTA (each half holds one superblock); *total = the half's sum.
-__device__ __forceinline__ uint64_t half_exclusive_scan(uint64_t x, uint64_t* total) {
-  __shared__ uint64_t ws[32];
-  uint32_t const lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  uint64_t inc = x;
-#pragma unroll
-  for (uint32_t o = 1; o < 32; o <<= 1) {
-    uint64_t const y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-    if (lane >= o) inc += y;
-  }
-  if (lane == 31) ws[wid] = inc;
-  __syncthreads();
-  if (wid == 0) {
-    uint64_t t = ws[lane];
-#pragma unroll
-    for (uint32_t o = 1; o < 16; o <<= 1) {  // scan within each 16-warp half
-      uint64_t const y = __shfl_up_sync(0xFFFFFFFFu, t, o);
-      if ((lane & 15) >= o) t += y;
-    }
-    ws[lane] = t;
-  }
-  __syncthreads();
-  uint64_t const before = (wid & 15) ? ws[wid - 1] : 0;
-  *total = ws[(wid & 16) + 15];
-  __syncthreads();
-  return before + inc - x;
-}
-
-// half_exclusive_scan for 32-bit values.
-__device__ __forceinline__ uint32_t half_exclusive_scan32(uint32_t x, uint32_t* total) {
-  __shared__ uint32_t ws32[32];
-  uint32_t const lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+// Exclusive scan over the 512 threads of one half of a 1024-thread CTA
+// (each half works on its own superblocks and synchronises on its own named
+// barrier, 1 or 2, so the halves overlap); *total = the half's sum.
+__device__ __forceinline__ uint32_t group_exclusive_scan32(uint32_t x, uint32_t* total) {
+  __shared__ uint32_t ws32[2][17];
+  uint32_t const lane = threadIdx.x & 31, wid = (threadIdx.x >> 5) & 15;
+  uint32_t const g = threadIdx.x >> 9;
+  uint32_t* const ws = ws32[g];
   uint32_t inc = x;
 #pragma unroll
   for (uint32_t o = 1; o < 32; o <<= 1) {
     uint32_t const y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
     if (lane >= o) inc += y;
   }
-  if (lane == 31) ws32[wid] = inc;
-  __syncthreads();
+  if (lane == 31) ws[wid] = inc;
+  asm volatile("bar.sync %0, 512;" ::"r"(g + 1) : "memory");
   if (wid == 0) {
-    uint32_t t = ws32[lane];
+    uint32_t t = lane < 16 ? ws[lane] : 0u;
 #pragma unroll
     for (uint32_t o = 1; o < 16; o <<= 1) {
       uint32_t const y = __shfl_up_sync(0xFFFFFFFFu, t, o);
-      if ((lane & 15) >= o) t += y;
+      if (lane >= o) t += y;
     }
-    ws32[lane] = t;
+    if (lane < 16) ws[lane] = t;  // inclusive over the half's warps
   }
-  __syncthreads();
-  uint32_t const before = (wid & 15) ? ws32[wid - 1] : 0;
-  *total = ws32[(wid & 16) + 15];
-  __syncthreads();
+  asm volatile("bar.sync %0, 512;" ::"r"(g + 1) : "memory");
+  uint32_t const before = wid ? ws[wid - 1] : 0u;
+  *total = ws[15];
+  asm volatile("bar.sync %0, 512;" ::"r"(g + 1) : "memory");
   return before + inc - x;
 }
 
-// Pass 3: persistent CTAs of 1024 threads, two superblocks at a time (one
-// per 512-thread half, one thread per 96-digit block), the digit table in
-// shared memory.
+// Pass 3: persistent CTAs of 1024 threads; each 512-thread half walks its
+// own superblocks (one thread per 96-digit block), the digit table shared
+// in shared memory.
 __global__ void __launch_bounds__(1024, 1)
 quad_level_kernel(TreeView v, uint32_t j, QuadLevel ql,
                   uint32_t const* __restrict__ hi_w, uint64_t hi_words,
@@ -382,12 +357,12 @@ quad_level_kernel(TreeView v, uint32_t j, QuadLevel ql,
   uint32_t const l = 2 * j, sh = v.levels - l;
   uint64_t const nodes = uint64_t(1) << l;
   uint32_t const t = threadIdx.x & (kQuadSbBlocks - 1);  // block inside its superblock
-  for (uint64_t pair = blockIdx.x; pair * 2 < nsb; pair += gridDim.x) {
-    uint64_t const sbi = pair * 2 + (threadIdx.x >> 9);
-    bool const live = sbi < nsb;
-    SbStart const st = info[live ? sbi : 0];
+  // half h of CTA b takes superblocks 2b + h, 2b + h + 2G, ...
+  uint64_t const first = uint64_t(blockIdx.x) * 2 + (threadIdx.x >> 9);
+  for (uint64_t sbi = first; sbi < nsb; sbi += uint64_t(gridDim.x) * 2) {
+    SbStart const st = info[sbi];
     uint64_t const blk = sbi * kQuadSbBlocks + t;
-    bool const mine = live && blk < ql.num_blocks;
+    bool const mine = blk < ql.num_blocks;
     uint64_t const p = blk * kQuadDigits;
     uint32_t h[3], vm[3];
     uint32_t ones = 0;
@@ -404,7 +379,7 @@ quad_level_kernel(TreeView v, uint32_t j, QuadLevel ql,
     uint32_t tot = 0;
     // ones of level 2j in the superblock before this block (= its digits 2
     // and 3 before it)
-    uint32_t const h23 = half_exclusive_scan32(ones, &tot);
+    uint32_t const h23 = group_exclusive_scan32(ones, &tot);
     uint64_t r1 = st.rank1 + h23;  // ones before p
     uint32_t dw[6] = {0, 0, 0, 0, 0, 0};
     uint64_t const right = st.node.start + st.node.zeros;  // right child start
@@ -457,8 +432,7 @@ quad_level_kernel(TreeView v, uint32_t j, QuadLevel ql,
       c1 += __popc(lo & ~hi);
     }
     uint32_t tot13 = 0;
-    uint32_t const h13 = half_exclusive_scan32(c1 | (c3 << 16), &tot13);  // each < 2^16
-    if (!live) continue;
+    uint32_t const h13 = group_exclusive_scan32(c1 | (c3 << 16), &tot13);  // each < 2^16
     uint64_t const* sbe = sb + sbi * 4;
     uint32_t const in_sb = t * kQuadDigits;  // positions before the block
     uint32_t const h1 = h13 & 0xFFFFu, h3 = h13 >> 16;
