@@ -161,6 +161,11 @@ namespace ewt {
 // Host orchestration of one tree build (wt_build.cu).
 void build_tree(ewt_tree& t, const void* data, uint64_t n, int elem_size,
                 const void* alphabet, uint64_t sigma, cudaStream_t stream);
+// Builds on this thread skip the device-wide synchronisation that orders a
+// device-resident text after the caller's work while set (a batch of builds
+// synchronises once before it starts; wt_build.cu).
+void set_texts_synchronized(bool v);
+bool texts_synchronized();
 // Sets t.view from the tree's device buffers and shape (wt_build.cu).
 void fill_tree_view(ewt_tree& t);
 

@@ -49,7 +49,7 @@ constexpr uint32_t kMultiChunk = 2048;
 constexpr uint32_t kMultiThreads = 256;
 constexpr uint32_t kPlanThreads = 1024;
 constexpr uint32_t kMaxMultiTrees = 1u << 16;  // trees in one call
-constexpr uint32_t kBuildWorkers = 8;          // host threads of a batch build
+constexpr uint32_t kBuildWorkers = 8;           // host threads of a batch build
 
 __global__ void __launch_bounds__(256)
 tree_hist_kernel(uint32_t const* __restrict__ tree_of, uint64_t m,
@@ -589,13 +589,36 @@ extern "C" int ewt_build_batch(const void* const* texts, const uint64_t* lengths
     EWT_REQUIRE(texts && lengths && out && count > 0, EWT_ERR_INVALID_ARGUMENT,
                 "texts, lengths and out must be given");
     for (uint32_t i = 0; i < count; ++i) out[i] = nullptr;
+    {
+      // Grow the library pool once for the whole batch (about four bytes
+      // of trees and build scratch per text byte): the builds then carve
+      // their buffers out of it instead of each growing the pool.
+      DeviceGuard g(gpu_index);
+      uint64_t need = 0;
+      for (uint32_t i = 0; i < count; ++i)
+        need += lengths[i] * uint64_t(elem_size > 0 ? elem_size : 1) * 4 + (uint64_t(2) << 20);
+      size_t free_b = 0, total_b = 0;
+      if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && need < free_b / 2) {
+        void* p = nullptr;
+        if (cudaMallocFromPoolAsync(&p, need, lib_pool(), nullptr) == cudaSuccess) {
+          cudaFreeAsync(p, nullptr);
+          cudaStreamSynchronize(nullptr);
+        }
+      }
+      (void)cudaGetLastError();  // best effort
+    }
     uint32_t const hw = std::max(1u, std::thread::hardware_concurrency());
     uint32_t const workers = std::min({count, kBuildWorkers, hw});
     std::atomic<uint32_t> next{0};
     std::mutex mu;
     int first_status = EWT_OK;
     std::string first_msg;
+    {  // device-resident texts: ordered after the caller's work once
+      DeviceGuard g(gpu_index);
+      EWT_CUDA(cudaDeviceSynchronize());
+    }
     auto work = [&] {
+      set_texts_synchronized(true);
       for (uint32_t i = next++; i < count; i = next++) {
         int const st = ewt_build(texts[i], lengths[i], elem_size,
                                  alphabets ? alphabets[i] : nullptr,
@@ -609,6 +632,7 @@ extern "C" int ewt_build_batch(const void* const* texts, const uint64_t* lengths
           }
         }
       }
+      set_texts_synchronized(false);
     };
     std::vector<std::thread> pool;
     for (uint32_t w = 1; w < workers; ++w) pool.emplace_back(work);

@@ -523,6 +523,8 @@ void run_passes(ewt_tree& t, T const* sym, uint64_t n, uint32_t* err,
   }
 }
 
+thread_local bool t_texts_synced = false;
+
 template <class T>
 void build_typed(ewt_tree& t, const void* data, uint64_t n,
                  const void* alphabet, uint64_t sigma, cudaStream_t st) {
@@ -531,8 +533,9 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   T const* d_text;
   bool const on_device = is_device_pointer(data);
   // The text may still be in flight on the caller's streams; the build runs
-  // on its own stream, so order it after all prior device work.
-  if (on_device) EWT_CUDA(cudaDeviceSynchronize());
+  // on its own stream, so order it after all prior device work (once per
+  // batch when a batch of builds already did).
+  if (on_device && !texts_synchronized()) EWT_CUDA(cudaDeviceSynchronize());
   if (on_device && reinterpret_cast<uintptr_t>(data) % 16 == 0) {
     d_text = static_cast<T const*>(data);
   } else if (on_device) {
@@ -815,6 +818,9 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
 }
 
 }  // namespace
+
+void set_texts_synchronized(bool v) { t_texts_synced = v; }
+bool texts_synchronized() { return t_texts_synced; }
 
 void fill_tree_view(ewt_tree& t) {
   TreeView& v = t.view;
