@@ -758,7 +758,24 @@ def run_ours(args, world, rank, local):
         + timed(lambda: tree.select_device(sq.data_ptr(), sq.shape[0],
                                            o_s.data_ptr(), sptr)))
     assert tree.query_status(sptr) == 0
+    # random-access roofline: dependent random 32-byte reads per second
+    probe = E.probe_random_reads(8 * GIB, 4, 1 << 25, local)
+    L_ = int(tree.info.levels)
+    steps = L_ // 2 + (L_ & 1)  # quad levels (+ an odd binary level)
+    reads = {"access": steps, "rank": steps, "select": 2 * steps}
+    reads["mixed"] = 0.4 * reads["access"] + 0.4 * reads["rank"] + 0.2 * reads["select"]
+    rates = {"access": acc_idx.numel() / acc_ms / 1e3 * 1e6,
+             "rank": rq.shape[0] / rank_ms / 1e3 * 1e6,
+             "select": sq.shape[0] / sel_ms / 1e3 * 1e6,
+             "mixed": m / mixed_ms / 1e3 * 1e6}
+    rroof = {"probe_reads_per_s": probe,
+             "model": "block reads per query: one per quad level for access and "
+                      "rank, a sample and a block per level for select (a lower "
+                      "bound: wide brackets read more)",
+             "reads_per_query": reads,
+             "frac": {k: rates[k] * reads[k] / probe for k in reads}}
     queries = {
+        "random_read_roofline": rroof,
         "autotuned": {"shapes": {k: [v["threads"], v["blocks_per_sm"]]
                                  for k, v in tuning.items() if k in KINDS},
                       "select_sample_rate": tuning["select_sample_rate"],

@@ -135,6 +135,8 @@ SIGNATURES = {
                                          C.c_void_p, C.c_void_p, C.c_void_p]),
     "ewt_autotune": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Tuning)]),
     "ewt_set_select_samples": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "ewt_probe_random_reads": (C.c_int, [C.c_int, C.c_uint64, C.c_uint32,
+                                         C.c_uint64, C.POINTER(C.c_double)]),
     "ewt_rs_set_select_samples": (C.c_int, [C.c_void_p, C.c_uint32]),
     "ewt_launch_count": (C.c_uint64, []),
     "ewt_set_timing": (None, [C.c_int]),
@@ -198,6 +200,16 @@ def _ptr(a: np.ndarray) -> int:
 
 def launch_count() -> int:
     return int(lib().ewt_launch_count())
+
+
+def probe_random_reads(bytes_: int = 8 << 30, depth: int = 4,
+                       chains: int = 1 << 25, gpu_index: int = 0) -> float:
+    """Dependent random 32-byte reads per second (ewt_probe_random_reads):
+    the random-access roofline of the query walks."""
+    r = C.c_double()
+    _check(lib().ewt_probe_random_reads(gpu_index, bytes_, depth, chains,
+                                        C.byref(r)), "probe_random_reads")
+    return r.value
 
 
 def release_cached_memory(gpu_index: int = 0):

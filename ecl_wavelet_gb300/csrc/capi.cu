@@ -758,6 +758,26 @@ void ewt_get_timing(ewt_phase_times* out, int reset) {
 const char* ewt_last_error(void) { return g_last_error.c_str(); }
 int ewt_abi_version(void) { return EWT_ABI_VERSION; }
 
+int ewt_probe_random_reads(int gpu_index, uint64_t bytes, uint32_t depth,
+                           uint64_t chains, double* reads_per_s) {
+  return guarded([&] {
+    EWT_REQUIRE(reads_per_s != nullptr, EWT_ERR_INVALID_ARGUMENT, "null argument");
+    DeviceGuard g(gpu_index);
+    cudaStream_t st = nullptr;
+    EWT_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    try {
+      AllocStream as(st);
+      probe_random_reads(bytes, depth, chains, reads_per_s);
+    } catch (...) {
+      cudaStreamSynchronize(st);
+      cudaStreamDestroy(st);
+      throw;
+    }
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+  });
+}
+
 int ewt_autotune(ewt_tree* t, uint64_t probe_queries, ewt_tuning* out) {
   return guarded([&] {
     EWT_REQUIRE(t != nullptr, EWT_ERR_INVALID_ARGUMENT, "tree is null");

@@ -210,6 +210,10 @@ void build_quad_samples(ewt_tree& t, uint32_t shift, cudaStream_t st);
 // Dense select samples of the binary and quad levels at rate 2^shift (0:
 // none), and the tree's view updated.
 void set_select_rate(ewt_tree& t, uint32_t shift, cudaStream_t st);
+// Random-access roofline: dependent random 32-byte reads per second over a
+// buffer of `bytes` (queries.cu).
+void probe_random_reads(uint64_t bytes, uint32_t depth, uint64_t chains,
+                        double* reads_per_s);
 // Times candidate launch shapes of every query kind on probe queries and
 // keeps the fastest in the tree (queries.cu).
 void autotune_queries(ewt_tree& t, uint64_t probe_queries, ewt_tuning* out);

@@ -415,7 +415,7 @@ void launch_mixed_raw(ewt_tree& t, uint8_t const* d_types, void const* d_q,
   }
 }
 
-// ---- autotuner -------------------------------------------------------------
+// ---- random-access roofline probe -------------------------------------------
 namespace {
 
 __device__ __forceinline__ uint64_t probe_mix(uint64_t x) {  // splitmix64
@@ -424,6 +424,62 @@ __device__ __forceinline__ uint64_t probe_mix(uint64_t x) {  // splitmix64
   x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
   return x ^ (x >> 31);
 }
+
+// Chains of `depth` dependent random 32-byte reads (two 16-byte loads, as a
+// query walk reads a block) over `units` 32-byte units; one chain per
+// thread and iteration.
+__global__ void __launch_bounds__(256)
+random_chain_kernel(uint4 const* __restrict__ a, uint64_t units, uint32_t depth,
+                    uint64_t chains, uint64_t* __restrict__ sink) {
+  uint64_t acc = 0;
+  uint64_t const stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t q = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; q < chains;
+       q += stride) {
+    uint64_t h = probe_mix(q + 0x1234567ull);
+    for (uint32_t d = 0; d < depth; ++d) {
+      uint4 const* u = a + (h % units) * 2;
+      uint4 const x = __ldg(u), y = __ldg(u + 1);
+      h = probe_mix(h ^ x.x ^ y.w);
+    }
+    acc += h;
+  }
+  if (acc == 0x5eedull) sink[0] = acc;  // keeps the loads
+}
+
+}  // namespace
+
+void probe_random_reads(uint64_t bytes, uint32_t depth, uint64_t chains,
+                        double* reads_per_s) {
+  EWT_REQUIRE(bytes >= (uint64_t(1) << 20) && depth >= 1 && depth <= 64 &&
+                  chains >= 1024,
+              EWT_ERR_INVALID_ARGUMENT, "probe: bytes >= 1 MiB, depth 1..64");
+  cudaStream_t s = alloc_stream();
+  DevBuf buf(bytes), sink(8);
+  EWT_CUDA(cudaMemsetAsync(buf.get(), 0x5a, bytes, s));
+  uint64_t const units = bytes / 32;
+  uint32_t const grid = static_cast<uint32_t>(sm_count()) * 4;
+  cudaEvent_t e0, e1;
+  EWT_CUDA(cudaEventCreate(&e0));
+  EWT_CUDA(cudaEventCreate(&e1));
+  random_chain_kernel<<<grid, 256, 0, s>>>(buf.as<uint4>(), units, depth, chains,
+                                           sink.as<uint64_t>());  // warm-up
+  EWT_LAUNCHED();
+  EWT_CUDA(cudaEventRecord(e0, s));
+  random_chain_kernel<<<grid, 256, 0, s>>>(buf.as<uint4>(), units, depth, chains,
+                                           sink.as<uint64_t>());
+  EWT_LAUNCHED();
+  EWT_CUDA(cudaEventRecord(e1, s));
+  EWT_CUDA(cudaEventSynchronize(e1));
+  float ms = 0;
+  EWT_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *reads_per_s = double(chains) * depth / (ms * 1e-3);
+}
+
+// ---- autotuner -------------------------------------------------------------
+namespace {
+
 
 // Valid probe queries over tree t: access i in [0, n); rank c uniform, i in
 // [0, n]; select c uniform, k in [1, count(c)] (k = 1 when c is absent);

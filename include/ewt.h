@@ -238,6 +238,14 @@ typedef struct ewt_tuning {
 } ewt_tuning;
 int ewt_autotune(ewt_tree* tree, uint64_t probe_queries, ewt_tuning* out);
 
+/* Random-access roofline of this GPU: dependent random 32-byte reads per
+ * second, `chains` chains of `depth` reads over a device buffer of `bytes`
+ * (larger than L2), read the way a query walk reads its blocks.  A query
+ * walk reading r blocks is bounded by reads_per_s / r queries per second.
+ * No reference counterpart (measurement utility). */
+int ewt_probe_random_reads(int gpu_index, uint64_t bytes, uint32_t depth,
+                           uint64_t chains, double* reads_per_s);
+
 /* Rebuilds the dense select samples (query side, beside the reference-format
  * samples, which exports keep) at one entry per `rate` zeros / ones: 0 drops
  * them (select then runs the reference's sample -> L1 -> L2 search, or on
