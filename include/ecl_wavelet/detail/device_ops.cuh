@@ -276,13 +276,22 @@ __device__ __forceinline__ uint64_t rs_select_dense(const RSView& v,
     uint32_t const h = __ldg(reinterpret_cast<uint32_t const*>(rb + mid * 2));
     if (before(mid, h) < i) lo = mid; else hi = mid - 1;
   }
-  uint4 const a0 = __ldg(rb + lo * 2), a1 = __ldg(rb + lo * 2 + 1);
-  uint4 const c0 = __ldg(rb + hi * 2), c1 = __ldg(rb + hi * 2 + 1);
-  uint64_t const bh = before(hi, c0.x);
-  bool const in_hi = hi > lo && bh < i;
-  uint4 const b0 = in_hi ? c0 : a0, b1 = in_hi ? c1 : a1;
-  uint64_t const t = in_hi ? hi : lo;
-  uint64_t const bt = in_hi ? bh : before(lo, a0.x);
+  // block lo first, block hi (= lo + 1) only when lo ends before the i-th
+  // value bit (query throughput follows the sectors read)
+  uint4 b0 = __ldg(rb + lo * 2), b1 = __ldg(rb + lo * 2 + 1);
+  uint64_t t = lo;
+  uint64_t bt = before(lo, b0.x);
+  if (hi > lo) {  // lo is a full block
+    uint32_t const ones_in = __popc(b0.y) + __popc(b0.z) + __popc(b0.w) +
+                             __popc(b1.x) + __popc(b1.y) + __popc(b1.z) + __popc(b1.w);
+    uint32_t const in = Value ? ones_in : uint32_t(kRankBlockBits) - ones_in;
+    if (bt + in < i) {
+      t = hi;
+      bt += in;
+      b0 = __ldg(rb + hi * 2);
+      b1 = __ldg(rb + hi * 2 + 1);
+    }
+  }
   uint32_t r = static_cast<uint32_t>(i - bt);  // 1 ..= kRankBlockBits
   uint32_t const w[kRankBlockWords] = {b0.y, b0.z, b0.w, b1.x,
                                        b1.y, b1.z, b1.w};
@@ -490,30 +499,29 @@ __device__ __forceinline__ uint64_t quad_select(const QuadView& v,
     uint64_t const mid = (lo + hi + 1) >> 1;
     if (before(mid) < k) lo = mid; else hi = mid - 1;
   }
-  // up to three blocks read at once; the last whose count before it is
-  // below k holds the k-th digit
-  uint64_t const mb = min(lo + 1, hi);
-  uint4 const a0 = __ldg(blocks + lo * 2), a1 = __ldg(blocks + lo * 2 + 1);
-  uint4 const b0 = __ldg(blocks + mb * 2), b1 = __ldg(blocks + mb * 2 + 1);
-  uint4 const c0 = __ldg(blocks + hi * 2), c1 = __ldg(blocks + hi * 2 + 1);
-  uint64_t const sa = __ldg(sb + (lo / kQuadSbBlocks) * 4);
-  uint64_t const sm = __ldg(sb + (mb / kQuadSbBlocks) * 4);
-  uint64_t const sc = __ldg(sb + (hi / kQuadSbBlocks) * 4);
-  uint64_t qa[4], qb[4], qc[4];
-  quad_words(a0, a1, qa);
-  quad_words(b0, b1, qb);
-  quad_words(c0, c1, qc);
-  uint64_t const bm = quad_before(qb[0], sm, d, mb);
-  uint64_t const bh = quad_before(qc[0], sc, d, hi);
-  int const which = (hi > mb && bh < k) ? 2 : (mb > lo && bm < k) ? 1 : 0;
-  uint64_t const blk = which == 2 ? hi : which == 1 ? mb : lo;
-  uint64_t const bt = which == 2 ? bh : which == 1 ? bm : quad_before(qa[0], sa, d, lo);
+  // forward from lo one block at a time (query throughput follows the
+  // sectors read): the block whose digits reach k holds the k-th one
+  uint64_t blk = lo;
+  uint64_t q[4];
+  {
+    uint4 const a0 = __ldg(blocks + lo * 2), a1 = __ldg(blocks + lo * 2 + 1);
+    quad_words(a0, a1, q);
+  }
+  uint64_t bt = quad_before(q[0], __ldg(sb + (lo / kQuadSbBlocks) * 4), d, lo);
+  while (blk < hi) {
+    uint64_t const in = quad_count(q, d, kQuadDigits);
+    if (bt + in >= k) break;
+    bt += in;
+    ++blk;
+    uint4 const a0 = __ldg(blocks + blk * 2), a1 = __ldg(blocks + blk * 2 + 1);
+    quad_words(a0, a1, q);
+  }
   uint32_t r = static_cast<uint32_t>(k - bt);  // 1 ..= 96
   uint32_t pos = 0;
   bool found = false;
 #pragma unroll
   for (uint32_t w = 1; w < 4; ++w) {
-    uint64_t const m = quad_match(which == 2 ? qc[w] : which == 1 ? qb[w] : qa[w], d);
+    uint64_t const m = quad_match(q[w], d);
     uint32_t const c = __popcll(m);
     if (!found) {
       if (r <= c) {
