@@ -63,6 +63,57 @@ tree_hist_kernel(uint32_t const* __restrict__ tree_of, uint64_t m,
   }
 }
 
+// Up to kSmemTrees trees: per-CTA shared-memory counts over a contiguous
+// slice of the batch (no global atomics per query), flushed once per CTA.
+constexpr uint32_t kSmemTrees = 4096;
+
+__global__ void __launch_bounds__(256)
+tree_hist_smem_kernel(uint32_t const* __restrict__ tree_of, uint64_t m,
+                      uint32_t num_trees, uint32_t* __restrict__ cnt) {
+  __shared__ uint32_t h[kSmemTrees + 1];
+  for (uint32_t i = threadIdx.x; i <= num_trees; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  uint64_t const per = (m + gridDim.x - 1) / gridDim.x;
+  uint64_t const s0 = min(m, blockIdx.x * per), s1 = min(m, s0 + per);
+  for (uint64_t q = s0 + threadIdx.x; q < s1; q += blockDim.x)
+    atomicAdd(&h[min(tree_of[q], num_trees)], 1u);  // num_trees: invalid id
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i <= num_trees; i += blockDim.x)
+    if (h[i]) atomicAdd(&cnt[i], h[i]);
+}
+
+// Query numbers into tree order for up to kSmemTrees trees: the CTA counts
+// its slice per tree, reserves one range per tree with a global atomic, and
+// hands out positions inside it from shared memory.
+__global__ void __launch_bounds__(256)
+tree_scatter_smem_kernel(uint32_t const* __restrict__ tree_of, uint64_t m,
+                         uint32_t num_trees, unsigned long long* __restrict__ cursor,
+                         uint32_t* __restrict__ perm, uint64_t* __restrict__ out,
+                         uint32_t* __restrict__ err) {
+  __shared__ uint32_t h[kSmemTrees];
+  for (uint32_t i = threadIdx.x; i < num_trees; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  uint64_t const per = (m + gridDim.x - 1) / gridDim.x;
+  uint64_t const s0 = min(m, blockIdx.x * per), s1 = min(m, s0 + per);
+  for (uint64_t q = s0 + threadIdx.x; q < s1; q += blockDim.x) {
+    uint32_t const t = tree_of[q];
+    if (t < num_trees) atomicAdd(&h[t], 1u);
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < num_trees; i += blockDim.x)
+    if (h[i]) h[i] = static_cast<uint32_t>(atomicAdd(&cursor[i], h[i]));  // perm is < 2^32
+  __syncthreads();
+  for (uint64_t q = s0 + threadIdx.x; q < s1; q += blockDim.x) {
+    uint32_t const t = tree_of[q];
+    if (t >= num_trees) {
+      out[q] = UINT64_MAX;
+      atomicOr(err, 2u);
+      continue;
+    }
+    perm[atomicAdd(&h[t], 1u)] = static_cast<uint32_t>(q);
+  }
+}
+
 // One CTA: tree starts in the tree-ordered batch (cursor) and the work list.
 __global__ void __launch_bounds__(kPlanThreads)
 tree_plan_kernel(uint32_t const* __restrict__ cnt, uint32_t num_trees,
@@ -457,16 +508,25 @@ void multi_device(ViewSet const& vs, uint32_t num_trees, uint32_t const* d_tree_
   uint32_t const grid = static_cast<uint32_t>(
       std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(m, 256), uint64_t(sm_count()) * 8)));
   PhaseTimer pt(EWT_PHASE_QUERY, s);
-  tree_hist_kernel<<<grid, 256, 0, s>>>(d_tree_of, m, num_trees, cnt.as<uint32_t>());
+  bool const smem_groups = num_trees <= kSmemTrees;
+  if (smem_groups)
+    tree_hist_smem_kernel<<<grid, 256, 0, s>>>(d_tree_of, m, num_trees, cnt.as<uint32_t>());
+  else
+    tree_hist_kernel<<<grid, 256, 0, s>>>(d_tree_of, m, num_trees, cnt.as<uint32_t>());
   EWT_LAUNCHED();
   tree_plan_kernel<<<1, kPlanThreads, 0, s>>>(cnt.as<uint32_t>(), num_trees,
                                               cursor.as<uint64_t>(),
                                               items.as<MultiItem>(),
                                               nitems.as<uint32_t>());
   EWT_LAUNCHED();
-  tree_scatter_kernel<<<grid, 256, 0, s>>>(
-      d_tree_of, m, num_trees, cursor.as<unsigned long long>(),
-      perm.as<uint32_t>(), d_out, d_err);
+  if (smem_groups)
+    tree_scatter_smem_kernel<<<grid, 256, 0, s>>>(
+        d_tree_of, m, num_trees, cursor.as<unsigned long long>(),
+        perm.as<uint32_t>(), d_out, d_err);
+  else
+    tree_scatter_kernel<<<grid, 256, 0, s>>>(
+        d_tree_of, m, num_trees, cursor.as<unsigned long long>(),
+        perm.as<uint32_t>(), d_out, d_err);
   EWT_LAUNCHED();
   launch_multi(vs.elem_size, vs.views.as<TreeView>(), items.as<MultiItem>(),
                nitems.as<uint32_t>(), 0, max_items, vs.max_levels,
