@@ -99,3 +99,27 @@ def test_mixed_multi_unknown_tree_and_device_form(ewt, oracle):
     assert int(d_err.item()) == 0
     got = d_out.cpu().numpy().view(np.uint64)
     assert np.array_equal(got, ewt.mixed_multi(trees, tree_of, types, q))
+
+
+def test_mixed_multi_many_trees(ewt, oracle):
+    """More trees than the shared-memory grouping holds (4,096): the batch is
+    grouped with global atomics instead and still answers every query as the
+    plain scan of its own text."""
+    rng = np.random.default_rng(24)
+    count = 4200
+    texts = [rng.integers(0, 4, int(rng.integers(50, 300)), dtype=np.uint64)
+             .astype(np.uint8) for _ in range(count)]
+    alphabets = [np.arange(4)] * count
+    trees = ewt.build_batch(texts, alphabets)
+    tree_of, types, index, sym = interleaved_queries(rng, trees, texts,
+                                                     alphabets, 20)
+    q = trees[0].make_queries(index, sym)
+    got = ewt.mixed_multi(trees, tree_of, types, q)
+    for i in range(0, count, 97):  # a spread of trees checked on the CPU
+        sel = tree_of == i
+        want, st = oracle.OracleTree(texts[i], alphabets[i]).mixed(
+            types[sel], index[sel], sym[sel])
+        assert st == 0
+        assert np.array_equal(got[sel], want), i
+    for t in trees:
+        t.close()
