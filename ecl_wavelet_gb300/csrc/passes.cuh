@@ -207,6 +207,96 @@ digit_count_kernel(T const* __restrict__ x, PassArgs p) {
   }
 }
 
+// 2'. Host texts read by the kernel (the first pass only, a = 0: one node,
+//     chunks of kPChunk symbols from the text start): each CTA copies whole
+//     chunks of the host text into device memory, writes level 0 (the top
+//     bit of every symbol) and counts the pass's digits per chunk -- the
+//     copy, the level-0 fill and the first digit count in one read of the
+//     host text.  Symbols at or above 2^L set bit 0 of err.
+template <class T>
+__global__ void __launch_bounds__(kPThreads)
+ingest_kernel(T const* __restrict__ host, T* __restrict__ dev,
+              uint32_t* __restrict__ level0, PassArgs p) {
+  __shared__ uint32_t cnt[kPMaxDigits * kPThreads];
+  __shared__ uint32_t tot[kPMaxDigits];
+  constexpr uint32_t kSym = 32;  // symbols per thread step: one level-0 word
+  constexpr uint32_t kVec = kSym * sizeof(T) / 16;
+  uint32_t const tid = threadIdx.x;
+  uint32_t const digits = 1u << p.k;
+  uint32_t const dshift = p.L - p.k, dmask = digits - 1;
+  uint32_t const total = p.chunk_first[p.nodes];
+  // bits at or above L in every symbol lane of a 32-bit word
+  uint32_t const hi_lanes = sizeof(T) == 1
+                                ? ((0xFFu << p.L) & 0xFFu) * 0x01010101u
+                                : ((0xFFFFu << p.L) & 0xFFFFu) * 0x00010001u;
+  uint32_t bad = 0;
+  for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
+    if (tid < kPMaxDigits) tot[tid] = 0;
+    for (uint32_t d = 0; d < digits; ++d) cnt[d * kPThreads + tid] = 0;
+    __syncthreads();
+    uint64_t const s = uint64_t(c) * kPChunk;
+    uint64_t const e = min(p.n, s + kPChunk);
+    for (uint64_t u = s / kSym + tid; u * kSym < e; u += kPThreads) {
+      uint64_t const p0 = u * kSym;
+      uint32_t const valid = static_cast<uint32_t>(min(uint64_t(kSym), e - p0));
+      uint32_t w[kSym * sizeof(T) / 4];
+      if (valid == kSym) {
+        uint4 const* src = reinterpret_cast<uint4 const*>(host + p0);
+        uint4* dst = reinterpret_cast<uint4*>(dev + p0);
+#pragma unroll
+        for (uint32_t i = 0; i < kVec; ++i) {
+          uint4 const x = src[i];
+          dst[i] = x;
+          w[4 * i] = x.x;
+          w[4 * i + 1] = x.y;
+          w[4 * i + 2] = x.z;
+          w[4 * i + 3] = x.w;
+        }
+      } else {
+#pragma unroll
+        for (uint32_t i = 0; i < kSym * sizeof(T) / 4; ++i) w[i] = 0;
+        for (uint32_t i = 0; i < valid; ++i) {
+          T const v = host[p0 + i];
+          dev[p0 + i] = v;
+          w[(i * sizeof(T)) >> 2] |= uint32_t(v) << (8 * ((i * sizeof(T)) & 3));
+        }
+      }
+      uint32_t bits = 0, over = 0;
+      uint32_t const top = p.L - 1;
+#pragma unroll
+      for (uint32_t i = 0; i < kSym * sizeof(T) / 4; ++i) {
+        if constexpr (sizeof(T) == 1) {
+          uint32_t const t1 = (w[i] >> top) & 0x01010101u;
+          bits |= (((t1 * 0x00204081u) >> 21) & 0xFu) << (4 * i);
+        } else {
+          uint32_t const t1 = (w[i] >> top) & 0x00010001u;
+          bits |= ((t1 | (t1 >> 15)) & 3u) << (2 * i);
+        }
+        over |= w[i] & hi_lanes;
+        // digits of the first pass: the top k bits
+#pragma unroll
+        for (uint32_t h = 0; h < 4 / sizeof(T); ++h) {
+          uint32_t const sym = (w[i] >> (8 * sizeof(T) * h)) & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu);
+          if (i * (4 / sizeof(T)) + h < valid) ++cnt[((sym >> dshift) & dmask) * kPThreads + tid];
+        }
+      }
+      bad |= over;
+      level0[u] = bits;  // bits past the text end are zero
+    }
+    __syncthreads();
+    for (uint32_t d = 0; d < digits; ++d) {
+      uint32_t v2 = cnt[d * kPThreads + tid];
+      for (int o = 16; o > 0; o >>= 1) v2 += __shfl_down_sync(0xffffffffu, v2, o);
+      if ((tid & 31) == 0) atomicAdd(&tot[d], v2);
+    }
+    __syncthreads();
+    if (tid < kPMaxDigits)
+      p.chunk_tot[uint64_t(c) * kPMaxDigits + tid] = tid < digits ? tot[tid] : 0u;
+    __syncthreads();
+  }
+  if (bad) atomicOr(p.err, 1u);
+}
+
 // 3. One CTA of 1024 threads per (level-a node, digit): exclusive counts of
 //    the digit before each chunk of the node (8 consecutive chunks per
 //    thread and step, block scan), and the node's total of the digit.

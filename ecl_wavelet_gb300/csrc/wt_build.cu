@@ -448,7 +448,7 @@ namespace {
 // ceil((L-1)/4) passes of near-equal size.
 template <class T>
 void run_passes(ewt_tree& t, T const* sym, uint64_t n, uint32_t* err,
-                cudaStream_t st) {
+                cudaStream_t st, T const* ingest_host = nullptr) {
   uint32_t const L = t.L;
   uint32_t const levels = L - 1;
   uint32_t const np = (levels + kPMaxK - 1) / kPMaxK;
@@ -499,9 +499,18 @@ void run_passes(ewt_tree& t, T const* sym, uint64_t n, uint32_t* err,
       PhaseTimer pt(EWT_PHASE_HIST, st);
       chunk_table_kernel<<<1, 1024, 0, st>>>(pa);
       EWT_LAUNCHED();
-      digit_count_kernel<T><<<static_cast<uint32_t>(std::min<uint64_t>(
-                                  max_chunks, uint64_t(sms) * 6)),
-                              kPThreads, 0, st>>>(cur, pa);
+      if (i == 0 && ingest_host) {
+        // the host text comes in here: copy, level 0 and first digit counts
+        PhaseTimer pt2(EWT_PHASE_H2D, st);
+        ingest_kernel<T><<<static_cast<uint32_t>(std::min<uint64_t>(
+                               max_chunks, uint64_t(sms) * 6)),
+                           kPThreads, 0, st>>>(ingest_host, const_cast<T*>(cur),
+                                               words + t.rs.meta[0].word_off, pa);
+      } else {
+        digit_count_kernel<T><<<static_cast<uint32_t>(std::min<uint64_t>(
+                                    max_chunks, uint64_t(sms) * 6)),
+                                kPThreads, 0, st>>>(cur, pa);
+      }
       EWT_LAUNCHED();
       pass_scan_kernel<<<pa.nodes << k, kScanThreads, 0, st>>>(pa);
       EWT_LAUNCHED();
@@ -525,12 +534,40 @@ void run_passes(ewt_tree& t, T const* sym, uint64_t n, uint32_t* err,
 
 thread_local bool t_texts_synced = false;
 
+// Whether a host text goes straight to the first pass's ingest kernel
+// (kernels read the host text: a Grace host's pageable memory, or pinned
+// memory): 1- and 2-byte symbols, a given minimal power-of-two alphabet of at
+// least four symbols, a 16-byte aligned text.
+template <class T>
+bool host_ingest(const void* data, uint64_t n, const void* alphabet, uint64_t sigma) {
+  if constexpr (sizeof(T) > 2) {
+    return false;
+  } else {
+    if (sigma < 4 || (sigma & (sigma - 1)) || !alphabet || n == 0 ||
+        reinterpret_cast<uintptr_t>(data) % 16)
+      return false;
+    T const* a = static_cast<T const*>(alphabet);
+    for (uint64_t i = 0; i < sigma; ++i)
+      if (uint64_t(a[i]) != i) return false;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    int pageable = 0;
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev);
+    cudaPointerAttributes pa{};
+    bool const pinned = cudaPointerGetAttributes(&pa, data) == cudaSuccess &&
+                        pa.type == cudaMemoryTypeHost;
+    (void)cudaGetLastError();
+    return pageable || pinned;
+  }
+}
+
 template <class T>
 void build_typed(ewt_tree& t, const void* data, uint64_t n,
                  const void* alphabet, uint64_t sigma, cudaStream_t st) {
   // ---- text on the device
   DevBuf text_owned;
   T const* d_text;
+  T const* ingest = nullptr;  // host text read by the first pass
   bool const on_device = is_device_pointer(data);
   // The text may still be in flight on the caller's streams; the build runs
   // on its own stream, so order it after all prior device work (once per
@@ -544,6 +581,11 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
     EWT_CUDA(cudaMemcpyAsync(text_owned.get(), data, n * sizeof(T),
                              cudaMemcpyDeviceToDevice, st));
     d_text = text_owned.as<T>();
+  } else if (host_ingest<T>(data, n, alphabet, sigma)) {
+    // read by the first pass's ingest kernel (see run_passes)
+    text_owned.alloc(n * sizeof(T) + 64);
+    d_text = text_owned.as<T>();
+    ingest = static_cast<T const*>(data);
   } else {
     text_owned.alloc(n * sizeof(T));
     PhaseTimer pt(EWT_PHASE_H2D, st);
@@ -715,9 +757,9 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   fill_tree_view(t);
   TreeView& v = t.view;
 
-  // ---- level 0 bits
+  // ---- level 0 bits (with an ingested host text: written by the first pass)
   uint32_t* const words = t.rs.words.as<uint32_t>();
-  {
+  if (!ingest) {
     PhaseTimer pt(EWT_PHASE_FILL, st);
     uint64_t const w0 = ceil_div(t.level_bits[0], 32);
     uint32_t const blocks =
@@ -734,7 +776,7 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   bool by_passes = false;
   if constexpr (sizeof(T) <= 2) {
     if (t.pow2 && L >= 2) {
-      run_passes<T>(t, sym, n, err_build, st);
+      run_passes<T>(t, sym, n, err_build, st, ingest);
       by_passes = true;
     }
   }
