@@ -563,7 +563,7 @@ void autotune_typed(ewt_tree& t, uint64_t m, ewt_tuning* out) {
       uint32_t const start = t.rs.ds.get() ? t.rs.sel_shift : 0;
       uint32_t best_sh = start;
       float best_ms = base;
-      for (uint32_t sh : {0u, 5u, 6u, 7u, 8u, 9u}) {
+      for (uint32_t sh : {0u, 6u, 7u, 8u, 9u, 10u}) {
         if (sh == start) continue;
         set_select_rate(t, sh, s);
         float const ms = timed();

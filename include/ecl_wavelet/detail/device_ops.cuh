@@ -67,7 +67,7 @@ constexpr uint32_t kRankHighShift = 24;
  * select reads two neighbouring entries, which bracket its block, and then
  * one or two rank blocks; sel_shift = 0 means none were built and select
  * uses the reference-format samples and counts. */
-constexpr uint32_t kDefaultSelShift = 6;
+constexpr uint32_t kDefaultSelShift = 8;
 
 /* rb_off / ds0_off of an array without rank blocks / dense samples (binary
  * levels that quad levels cover); rank and select then use L1/L2. */
@@ -271,26 +271,39 @@ __device__ __forceinline__ uint64_t rs_select_dense(const RSView& v,
     uint64_t const ones = rb_ones_before(v, m, k, h);
     return Value ? ones : k * kRankBlockBits - ones;
   };
-  while (hi - lo > 1) {  // wide brackets only (sparse values)
+  while (hi - lo > 16) {  // wide brackets only (sparse values)
     uint64_t const mid = (lo + hi + 1) >> 1;
     uint32_t const h = __ldg(reinterpret_cast<uint32_t const*>(rb + mid * 2));
     if (before(mid, h) < i) lo = mid; else hi = mid - 1;
   }
-  // block lo first, block hi (= lo + 1) only when lo ends before the i-th
-  // value bit (query throughput follows the sectors read)
-  uint4 b0 = __ldg(rb + lo * 2), b1 = __ldg(rb + lo * 2 + 1);
-  uint64_t t = lo;
-  uint64_t bt = before(lo, b0.x);
-  if (hi > lo) {  // lo is a full block
-    uint32_t const ones_in = __popc(b0.y) + __popc(b0.z) + __popc(b0.w) +
-                             __popc(b1.x) + __popc(b1.y) + __popc(b1.z) + __popc(b1.w);
-    uint32_t const in = Value ? ones_in : uint32_t(kRankBlockBits) - ones_in;
-    if (bt + in < i) {
-      t = hi;
-      bt += in;
-      b0 = __ldg(rb + hi * 2);
-      b1 = __ldg(rb + hi * 2 + 1);
+  // from the interpolated block, one block at a time (query throughput
+  // follows the sectors read): the block holding the i-th value bit has
+  // fewer than i of them before it and at least i up to its end
+  uint64_t t = hi - lo > 1 && hi - lo <= 16
+                   ? lo + (((hi - lo) * ((i - 1) - (j << sh))) >> sh)
+                   : lo;
+  uint4 b0, b1;
+  uint64_t bt = 0;
+  for (uint32_t guard = 0; guard < 24; ++guard) {
+    b0 = __ldg(rb + t * 2);
+    b1 = __ldg(rb + t * 2 + 1);
+    bt = before(t, b0.x);
+    if (bt >= i && t > lo) {  // it lies before this block
+      hi = t - 1;
+      --t;
+      continue;
     }
+    if (t < hi) {  // t is a full block
+      uint32_t const ones_in = __popc(b0.y) + __popc(b0.z) + __popc(b0.w) +
+                               __popc(b1.x) + __popc(b1.y) + __popc(b1.z) + __popc(b1.w);
+      uint32_t const in = Value ? ones_in : uint32_t(kRankBlockBits) - ones_in;
+      if (bt + in < i) {  // after it
+        lo = t + 1;
+        ++t;
+        continue;
+      }
+    }
+    break;
   }
   uint32_t r = static_cast<uint32_t>(i - bt);  // 1 ..= kRankBlockBits
   uint32_t const w[kRankBlockWords] = {b0.y, b0.z, b0.w, b1.x,
@@ -473,7 +486,7 @@ __device__ __forceinline__ uint64_t quad_select(const QuadView& v,
   if (k == 0 || k > ql.total[d]) return nblk * kQuadDigits;  // invalid structure
   uint64_t const* sb = v.sb + ql.sb_off * 4 + d;
   uint4 const* blocks = v.blocks + ql.blk_off * 2;
-  uint64_t lo, hi;
+  uint64_t lo, hi, est;
   if (v.ds) {
     uint32_t const sh = v.sel_shift;
     uint32_t const* S = v.ds + ql.ds_off[d];
@@ -481,6 +494,9 @@ __device__ __forceinline__ uint64_t quad_select(const QuadView& v,
     lo = min(uint64_t(__ldg(S + j)), nblk - 1);
     hi = ((j + 1) << sh) < ql.total[d] ? __ldg(S + j + 1) : nblk - 1;
     hi = min(max(hi, lo), nblk - 1);
+    // the k-th digit sits about (k - 1 - j * R) / R of the way into the
+    // bracket: start there
+    est = lo + (((hi - lo) * ((k - 1) - (j << sh))) >> sh);
   } else {  // superblock whose count before it is below k
     uint64_t a = 0, z = (nblk - 1) / kQuadSbBlocks;
     while (a < z) {
@@ -489,32 +505,39 @@ __device__ __forceinline__ uint64_t quad_select(const QuadView& v,
     }
     lo = a * kQuadSbBlocks;
     hi = min(lo + kQuadSbBlocks - 1, nblk - 1);
+    est = lo;
   }
   auto before = [&](uint64_t blk) -> uint64_t {
     uint4 const h = __ldg(blocks + blk * 2);
     return quad_before((uint64_t(h.y) << 32) | h.x,
                        __ldg(sb + (blk / kQuadSbBlocks) * 4), d, blk);
   };
-  while (hi - lo > 2) {  // wide brackets only (rare digits)
+  while (hi - lo > 16) {  // wide brackets only (rare digits)
     uint64_t const mid = (lo + hi + 1) >> 1;
     if (before(mid) < k) lo = mid; else hi = mid - 1;
+    est = lo;
   }
-  // forward from lo one block at a time (query throughput follows the
-  // sectors read): the block whose digits reach k holds the k-th one
-  uint64_t blk = lo;
+  // from the estimate, one block at a time (query throughput follows the
+  // sectors read): the block holding the k-th digit has fewer than k of them
+  // before it and at least k up to its end
+  uint64_t blk = min(max(est, lo), hi);
   uint64_t q[4];
-  {
-    uint4 const a0 = __ldg(blocks + lo * 2), a1 = __ldg(blocks + lo * 2 + 1);
-    quad_words(a0, a1, q);
-  }
-  uint64_t bt = quad_before(q[0], __ldg(sb + (lo / kQuadSbBlocks) * 4), d, lo);
-  while (blk < hi) {
-    uint64_t const in = quad_count(q, d, kQuadDigits);
-    if (bt + in >= k) break;
-    bt += in;
-    ++blk;
+  uint64_t bt = 0;
+  for (uint32_t guard = 0; guard < 24; ++guard) {
     uint4 const a0 = __ldg(blocks + blk * 2), a1 = __ldg(blocks + blk * 2 + 1);
     quad_words(a0, a1, q);
+    bt = quad_before(q[0], __ldg(sb + (blk / kQuadSbBlocks) * 4), d, blk);
+    if (bt >= k && blk > lo) {  // it lies before this block
+      hi = blk - 1;
+      --blk;
+      continue;
+    }
+    if (blk < hi && bt + quad_count(q, d, kQuadDigits) < k) {  // after it
+      lo = blk + 1;
+      ++blk;
+      continue;
+    }
+    break;
   }
   uint32_t r = static_cast<uint32_t>(k - bt);  // 1 ..= 96
   uint32_t pos = 0;

@@ -220,7 +220,7 @@ uint64_t ewt_launch_count(void);
  * Times the query kernels on probe_queries device-generated valid queries
  * over this tree and keeps the fastest configuration for every later query
  * on it: first the dense select-sample rate (every R-th zero / one, R in
- * {32, 64, 128, 256, 512}, or none: the reference-format samples alone), timed
+ * {64, 128, 256, 512, 1024}, or none: the reference-format samples alone), timed
  * on select probes, then per kind (access, rank, select, mixed) the launch
  * shape (threads per CTA x resident CTAs per SM).  *out (may be NULL)
  * reports the choices and the default and tuned rates.  Results never
@@ -250,7 +250,7 @@ int ewt_probe_random_reads(int gpu_index, uint64_t bytes, uint32_t depth,
  * samples, which exports keep) at one entry per `rate` zeros / ones: 0 drops
  * them (select then runs the reference's sample -> L1 -> L2 search, or on
  * quad levels a search of the superblock table), else a
- * power of two in [32, 65536]; each entry costs 4 bytes.  Built at 64 by
+ * power of two in [32, 65536]; each entry costs 4 bytes.  Built at 256 by
  * default.  Refused (EWT_ERR_INVALID_ARGUMENT) once the device view was
  * copied out.  No reference counterpart (rank_select.cuh:44-64 fixes one
  * sample per 4096 at compile time). */

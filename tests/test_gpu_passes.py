@@ -154,7 +154,7 @@ def test_autotuned_queries_exact(ewt, oracle, dtype, sigma, minimal):
     tuning = gt.autotune(1 << 14)
     assert set(tuning) == {"access", "rank", "select", "mixed",
                            "select_sample_rate"}
-    assert tuning["select_sample_rate"] in (0, 32, 64, 128, 256, 512)
+    assert tuning["select_sample_rate"] in (0, 64, 128, 256, 512, 1024)
     for kind in ("access", "rank", "select", "mixed"):
         r = tuning[kind]
         assert r["threads"] in (128, 256), (kind, r)
