@@ -6,6 +6,9 @@
 
 #include <atomic>
 #include <cstdint>
+#include <mutex>
+#include <set>
+#include <utility>
 #include <cstdio>
 #include <new>
 #include <stdexcept>
@@ -214,6 +217,22 @@ inline int sm_count() {
 }
 
 inline uint64_t ceil_div(uint64_t a, uint64_t b) { return (a + b - 1) / b; }
+
+// Raises kernel `f`'s dynamic shared-memory limit to `bytes` on the current
+// device, once per (kernel, device): the attribute belongs to the kernel's
+// instance in that device's context.
+template <class Kernel>
+void set_smem_limit(Kernel f, int bytes) {
+  static std::mutex mu;
+  static std::set<std::pair<void const*, int>> done;
+  int dev = 0;
+  EWT_CUDA(cudaGetDevice(&dev));
+  auto const key = std::make_pair(reinterpret_cast<void const*>(f), dev);
+  std::lock_guard<std::mutex> lk(mu);
+  if (done.count(key)) return;
+  EWT_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  done.insert(key);
+}
 
 // Puts this thread's stream-capture mode to relaxed for its scope, so that
 // the host-side launch preparation (kernel attributes, occupancy queries) of

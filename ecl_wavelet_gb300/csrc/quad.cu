@@ -582,13 +582,7 @@ void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, cudaStream_t st) {
   EWT_CUDA(cudaMemcpyAsync(lut_d.get(), lut.data(), lut.size() * 2,
                            cudaMemcpyHostToDevice, st));
   EWT_CUDA(cudaMemsetAsync(err_d.get(), 0, 4, st));
-  static bool const attr = [] {
-    EWT_CUDA(cudaFuncSetAttribute(quad_level_kernel,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  65536 * 2));
-    return true;
-  }();
-  (void)attr;
+  set_smem_limit(quad_level_kernel, 65536 * 2);
   uint64_t const max_nsb = ceil_div(n / kQuadDigits + 1, kQuadSbBlocks);
   DevBuf chunk(ceil_div(max_nsb + 1, kScanChunk) * 32);
   DevBuf info(max_nsb * sizeof(SbStart));

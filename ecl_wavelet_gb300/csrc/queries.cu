@@ -296,14 +296,7 @@ void launch_typed(ewt_tree& t, uint8_t const* types, void const* in,
   RelaxedCapture relaxed;  // these launches may be captured into a graph
   if (K == kMixed) {
     auto mk = mixed_kernel<T>;
-    static thread_local bool mattr[4] = {};
-    int const mi = sizeof(T) == 1 ? 0 : sizeof(T) == 2 ? 1 : sizeof(T) == 4 ? 2 : 3;
-    if (!mattr[mi]) {
-      EWT_CUDA(cudaFuncSetAttribute(
-          mk, cudaFuncAttributeMaxDynamicSharedMemorySize,
-          static_cast<int>(kStageLimitBytes + 4096)));
-      mattr[mi] = true;
-    }
+    set_smem_limit(mk, static_cast<int>(kStageLimitBytes + 4096));
     uint32_t const threads = t.tune_threads[K] ? t.tune_threads[K] : kQueryThreads;
     int per_sm = 0;
     EWT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mk,
@@ -322,13 +315,7 @@ void launch_typed(ewt_tree& t, uint8_t const* types, void const* in,
     return;
   }
   auto k = query_kernel<T, K>;
-  static thread_local bool attr_set[4][4] = {};
-  int const ti = sizeof(T) == 1 ? 0 : sizeof(T) == 2 ? 1 : sizeof(T) == 4 ? 2 : 3;
-  if (!attr_set[ti][K]) {
-    EWT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  static_cast<int>(kStageLimitBytes + 4096)));
-    attr_set[ti][K] = true;
-  }
+  set_smem_limit(k, static_cast<int>(kStageLimitBytes + 4096));
   uint32_t const threads = t.tune_threads[K] ? t.tune_threads[K] : kQueryThreads;
   int per_sm = 0;
   EWT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k,

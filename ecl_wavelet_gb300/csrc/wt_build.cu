@@ -521,9 +521,7 @@ void run_passes(ewt_tree& t, T const* sym, uint64_t n, uint32_t* err,
       PhaseTimer pt(EWT_PHASE_SPLIT, st);
       auto kern = write_order ? pass_kernel<T, true> : pass_kernel<T, false>;
       size_t const smem = pass_smem_bytes<T>();
-      EWT_CUDA(cudaFuncSetAttribute(
-          kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-          static_cast<int>(smem)));
+      set_smem_limit(kern, static_cast<int>(smem));
       kern<<<grid, kPThreads, smem, st>>>(cur, next, pa);
       EWT_LAUNCHED();
     }
