@@ -207,12 +207,12 @@ digit_count_kernel(T const* __restrict__ x, PassArgs p) {
   }
 }
 
-// 2'. Host texts read by the kernel (the first pass only, a = 0: one node,
-//     chunks of kPChunk symbols from the text start): each CTA copies whole
-//     chunks of the host text into device memory, writes level 0 (the top
-//     bit of every symbol) and counts the pass's digits per chunk -- the
-//     copy, the level-0 fill and the first digit count in one read of the
-//     host text.  Symbols at or above 2^L set bit 0 of err.
+// 2'. The first pass's read of the text (a = 0: one node, chunks of kPChunk
+//     symbols from the text start): each CTA takes whole chunks, writes
+//     level 0 (the top bit of every symbol) and counts the pass's digits per
+//     chunk, and for a host text (dev != null) also copies the chunk into
+//     device memory -- the level-0 fill, the first digit count and the copy
+//     in one read of the text.  Symbols at or above 2^L set bit 0 of err.
 template <class T>
 __global__ void __launch_bounds__(kPThreads)
 ingest_kernel(T const* __restrict__ host, T* __restrict__ dev,
@@ -246,7 +246,7 @@ ingest_kernel(T const* __restrict__ host, T* __restrict__ dev,
 #pragma unroll
         for (uint32_t i = 0; i < kVec; ++i) {
           uint4 const x = src[i];
-          dst[i] = x;
+          if (dev) dst[i] = x;
           w[4 * i] = x.x;
           w[4 * i + 1] = x.y;
           w[4 * i + 2] = x.z;
@@ -257,7 +257,7 @@ ingest_kernel(T const* __restrict__ host, T* __restrict__ dev,
         for (uint32_t i = 0; i < kSym * sizeof(T) / 4; ++i) w[i] = 0;
         for (uint32_t i = 0; i < valid; ++i) {
           T const v = host[p0 + i];
-          dev[p0 + i] = v;
+          if (dev) dev[p0 + i] = v;
           w[(i * sizeof(T)) >> 2] |= uint32_t(v) << (8 * ((i * sizeof(T)) & 3));
         }
       }

@@ -448,7 +448,8 @@ namespace {
 // ceil((L-1)/4) passes of near-equal size.
 template <class T>
 void run_passes(ewt_tree& t, T const* sym, uint64_t n, uint32_t* err,
-                cudaStream_t st, T const* ingest_host = nullptr) {
+                cudaStream_t st, T const* ingest_src = nullptr,
+                bool ingest_copy = false) {
   uint32_t const L = t.L;
   uint32_t const levels = L - 1;
   uint32_t const np = (levels + kPMaxK - 1) / kPMaxK;
@@ -499,12 +500,14 @@ void run_passes(ewt_tree& t, T const* sym, uint64_t n, uint32_t* err,
       PhaseTimer pt(EWT_PHASE_HIST, st);
       chunk_table_kernel<<<1, 1024, 0, st>>>(pa);
       EWT_LAUNCHED();
-      if (i == 0 && ingest_host) {
-        // the host text comes in here: copy, level 0 and first digit counts
-        PhaseTimer pt2(EWT_PHASE_H2D, st);
+      if (i == 0 && ingest_src) {
+        // level 0 and the first digit counts in one read of the text (and,
+        // for a host text, its copy to the device)
+        PhaseTimer pt2(ingest_copy ? EWT_PHASE_H2D : EWT_PHASE_FILL, st);
         ingest_kernel<T><<<static_cast<uint32_t>(std::min<uint64_t>(
                                max_chunks, uint64_t(sms) * 6)),
-                           kPThreads, 0, st>>>(ingest_host, const_cast<T*>(cur),
+                           kPThreads, 0, st>>>(ingest_src,
+                                               ingest_copy ? const_cast<T*>(cur) : nullptr,
                                                words + t.rs.meta[0].word_off, pa);
       } else {
         digit_count_kernel<T><<<static_cast<uint32_t>(std::min<uint64_t>(
@@ -536,17 +539,29 @@ thread_local bool t_texts_synced = false;
 // (kernels read the host text: a Grace host's pageable memory, or pinned
 // memory): 1- and 2-byte symbols, a given minimal power-of-two alphabet of at
 // least four symbols, a 16-byte aligned text.
+// A given alphabet 0 .. sigma-1 with sigma a power of two >= 4 (1- and
+// 2-byte symbols): the texts whose first pass can read them directly.
+template <class T>
+bool minimal_pow2_alphabet(const void* alphabet, uint64_t sigma) {
+  if constexpr (sizeof(T) > 2) {
+    return false;
+  } else {
+    if (sigma < 4 || (sigma & (sigma - 1)) || !alphabet) return false;
+    T const* a = static_cast<T const*>(alphabet);
+    for (uint64_t i = 0; i < sigma; ++i)
+      if (uint64_t(a[i]) != i) return false;
+    return true;
+  }
+}
+
 template <class T>
 bool host_ingest(const void* data, uint64_t n, const void* alphabet, uint64_t sigma) {
   if constexpr (sizeof(T) > 2) {
     return false;
   } else {
-    if (sigma < 4 || (sigma & (sigma - 1)) || !alphabet || n == 0 ||
+    if (!minimal_pow2_alphabet<T>(alphabet, sigma) || n == 0 ||
         reinterpret_cast<uintptr_t>(data) % 16)
       return false;
-    T const* a = static_cast<T const*>(alphabet);
-    for (uint64_t i = 0; i < sigma; ++i)
-      if (uint64_t(a[i]) != i) return false;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return false;
     int pageable = 0;
@@ -565,7 +580,8 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   // ---- text on the device
   DevBuf text_owned;
   T const* d_text;
-  T const* ingest = nullptr;  // host text read by the first pass
+  T const* ingest = nullptr;  // text read by the first pass's ingest kernel
+  bool ingest_copy = false;   // ... a host text, copied by it
   bool const on_device = is_device_pointer(data);
   // The text may still be in flight on the caller's streams; the build runs
   // on its own stream, so order it after all prior device work (once per
@@ -584,6 +600,7 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
     text_owned.alloc(n * sizeof(T) + 64);
     d_text = text_owned.as<T>();
     ingest = static_cast<T const*>(data);
+    ingest_copy = true;
   } else {
     text_owned.alloc(n * sizeof(T));
     PhaseTimer pt(EWT_PHASE_H2D, st);
@@ -774,7 +791,7 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   bool by_passes = false;
   if constexpr (sizeof(T) <= 2) {
     if (t.pow2 && L >= 2) {
-      run_passes<T>(t, sym, n, err_build, st, ingest);
+      run_passes<T>(t, sym, n, err_build, st, ingest, ingest_copy);
       by_passes = true;
     }
   }
