@@ -280,7 +280,8 @@ def test_device_resident_batches(ewt, oracle):
 
 
 @pytest.mark.parametrize("n,sigma", [((1 << 31) + 12345, 256),
-                                     ((1 << 32) + 777, 4)])
+                                     ((1 << 32) + 777, 4),
+                                     ((1 << 32) + 96 * 7 + 5, 256)])
 def test_large_text_round_trips(ewt, n, sigma):
     """n > 2^31 exercises 64-bit positions, n > 2^32 also level arrays
     longer than 2^24 rank blocks (their counts need the high-count table);
