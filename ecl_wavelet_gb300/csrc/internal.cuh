@@ -205,6 +205,9 @@ void prepare_serve_kernels(uint32_t elem_size);
 // and count table C (sigma + 1 entries), and a rebuild of their dense select
 // samples at rate 2^shift (0: none).
 bool quad_eligible(ewt_tree const& t);
+// Digit widths of the group levels of an L-level tree, top down: octal (3)
+// groups, then one or two quad (2) groups; they cover all L levels.
+std::vector<uint32_t> group_widths(uint32_t L);
 void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, cudaStream_t st);
 void build_quad_samples(ewt_tree& t, uint32_t shift, cudaStream_t st);
 // Dense select samples of the binary and quad levels at rate 2^shift (0:

@@ -2,7 +2,7 @@
 // rebuilding (ewt_save / ewt_load).  The reference has no serialisation; a
 // serving process uses this to admit prebuilt indexes.
 //
-// Layout (little-endian): the magic "EWTIDX02", a header of 64-bit fields,
+// Layout (little-endian): the magic "EWTIDX03", a header of 64-bit fields,
 // the host-side shape (alphabet, count table, codes, node starts, nodes per
 // level, node bases, level sizes, per-array metadata), then the device arrays
 // in a fixed order (level words, L1, L2, samples of zeros and ones, rank
@@ -19,7 +19,7 @@
 namespace ewt {
 namespace {
 
-constexpr char kMagic[8] = {'E', 'W', 'T', 'I', 'D', 'X', '0', '2'};
+constexpr char kMagic[8] = {'E', 'W', 'T', 'I', 'D', 'X', '0', '3'};
 constexpr size_t kPiece = size_t(64) << 20;
 
 struct File {
@@ -132,7 +132,7 @@ extern "C" int ewt_save(const ewt_tree* t, const char* path) {
     dev_to_file(f, t->rs.ds.get(), t->rs.ds.bytes(), stage, s);
     dev_to_file(f, t->counts_d.get(), t->counts_d.bytes(), stage, s);
     dev_to_file(f, t->ranks_d.get(), t->ranks_d.bytes(), stage, s);
-    // quad query levels (none for other alphabets)
+    // group query levels (none for other alphabets)
     f.put_vec(t->quad.levels);
     f.put(t->quad.ds.get() ? t->quad.sel_shift : 0);
     if (!t->quad.levels.empty()) {
@@ -209,11 +209,20 @@ extern "C" int ewt_load(const char* path, int gpu_index, ewt_tree** out) {
       file_to_dev(f, t->ranks_d, stage, s, big);
       t->quad.levels = f.get_vec<ecl::detail::QuadLevel>(t->L / 2 + 1);
       t->quad.sel_shift = static_cast<uint32_t>(f.get());
-      EWT_REQUIRE(t->quad.levels.empty() ||
-                      (t->quad.levels.size() == t->L / 2 && quad_eligible(*t) &&
-                       (t->quad.sel_shift == 0 ||
-                        (t->quad.sel_shift >= 5 && t->quad.sel_shift <= 16))),
-                  EWT_ERR_INVALID_ARGUMENT, "index file is corrupt");
+      bool plan_ok = t->quad.levels.empty() ||
+                     (quad_eligible(*t) && (t->quad.sel_shift == 0 ||
+                                            (t->quad.sel_shift >= 5 && t->quad.sel_shift <= 16)));
+      if (!t->quad.levels.empty()) {
+        std::vector<uint32_t> const widths = group_widths(t->L);
+        plan_ok = plan_ok && widths.size() == t->quad.levels.size();
+        uint32_t l = 0;
+        for (size_t j = 0; plan_ok && j < widths.size(); ++j) {
+          auto const& ql = t->quad.levels[j];
+          plan_ok = ql.width == widths[j] && ql.start == l && ql.sel_shift <= 16;
+          l += widths[j];
+        }
+      }
+      EWT_REQUIRE(plan_ok, EWT_ERR_INVALID_ARGUMENT, "index file is corrupt");
       if (!t->quad.levels.empty()) {
         file_to_dev(f, t->quad.blocks, stage, s, big);
         file_to_dev(f, t->quad.sb, stage, s, big);

@@ -1,21 +1,32 @@
-// Quad (4-ary) query levels of power-of-two trees: every pair of binary
-// levels (2j, 2j+1) becomes one level of 2-bit digits in level-2j order, so
-// a query resolves two binary levels per dependent DRAM access.  No
+// Group query levels of power-of-two trees: runs of w = 2 (quad) or 3
+// (octal) consecutive binary levels l .. l+w-1 become one level of w-bit
+// digits in level-l order, so a query resolves w binary levels per
+// dependent DRAM access.  The plan covers all L levels: as many octal
+// groups as fit, then one or two quad groups (L = 8: 3 + 3 + 2).  No
 // reference counterpart; the binary levels and their RankSelect stay the
-// source of truth for exports and are walked for an odd last level.
+// source of truth for exports.
 //
-// A level-2j node's zeros go, in order, to its left child on level 2j+1 and
-// its ones to its right child, so the low bits of a run of positions inside
-// one node are two runs of level 2j+1, merged by the high bits.  Per quad
-// level:
+// A level-l node's zeros go, in order, to its left child on level l+1 and
+// its ones to its right child, so the bits of level l+1 under a run of
+// positions inside one node are two runs of level l+1, merged by the bits of
+// level l ("routing" level l+1 into level-l order).
+// Quad group at l:
 //   1. quad_sb_count_kernel (thread per 512-block superblock): its digit
 //      counts from six ranks per node segment (no per-position work);
-//   2. quad_scan_*: counts before every superblock (chunked scan);
+//   2. group_scan_*: counts before every superblock (chunked scan);
 //   3. quad_level_kernel (persistent, two superblocks per 1024-thread CTA,
 //      one thread per 96-digit block): digits from the two runs, eight at a
 //      time through a 64K-entry table in shared memory, block headers from
 //      a scan, blocks and dense select samples written; the superblock's
 //      totals are checked against pass 1.
+// Octal group at l:
+//   1. merge_plane_kernel: level l+2 routed into level-(l+1) order (a plane
+//      of n bits);
+//   2. octal_level_kernel (same shape, one thread per 42-digit block): the
+//      digit's middle and low bits route level l+1 and that plane into
+//      level-l order; headers from a scan; per-superblock counts written;
+//   3. group_scan_*, then group_samples_kernel (dense samples; the level's
+//      digit totals checked against the count table).
 // Node ranks (digit counts before every node) and digit totals come from
 // the count table on the host.
 #include <algorithm>
@@ -25,11 +36,17 @@
 
 namespace ewt {
 
+using ecl::detail::GroupShape;
 using ecl::detail::kQuadDigits;
 using ecl::detail::kQuadSbBlocks;
 using ecl::detail::kQuadSbDigits;
 using ecl::detail::QuadLevel;
 using ecl::detail::QuadView;
+
+constexpr uint32_t kOctDigits = GroupShape<3>::kDigits;
+constexpr uint32_t kOctSbBlocks = GroupShape<3>::kSbBlocks;
+constexpr uint64_t kOctSbDigits = uint64_t(kOctDigits) * kOctSbBlocks;
+constexpr uint64_t kMergeSbPos = 512 * 64;  // positions per merge-kernel superblock
 
 namespace {
 
@@ -103,9 +120,9 @@ struct SbStart {
   uint64_t uniform;
 };
 
-// Pass 1: digit counts of every superblock (thread per superblock).
+// Quad pass 1: digit counts of every superblock (thread per superblock).
 __global__ void __launch_bounds__(128)
-quad_sb_count_kernel(TreeView v, uint32_t j, uint64_t nsb,
+quad_sb_count_kernel(TreeView v, uint32_t l, uint64_t nsb,
                      uint64_t* __restrict__ sb, SbStart* __restrict__ info) {
   uint64_t const s = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   if (s > nsb) return;
@@ -115,7 +132,7 @@ quad_sb_count_kernel(TreeView v, uint32_t j, uint64_t nsb,
   uint64_t const e = min(n, a + kQuadSbDigits);
   if (s < nsb && a >= e) info[s] = SbStart{QuadNode{0, n, 0, 0}, 0, 1};
   if (s < nsb && a < e) {
-    uint32_t const l = 2 * j, sh = v.levels - l;
+    uint32_t const sh = v.levels - l;
     uint64_t const nodes = uint64_t(1) << l;
     ArrayMeta const mh = v.rs.meta[l], ml = v.rs.meta[l + 1];
     uint64_t g = node_of(v.counts, sh, nodes, a);
@@ -180,85 +197,106 @@ __device__ __forceinline__ uint64_t cta_exclusive_scan(uint64_t x, uint64_t* tot
   return before + inc - x;
 }
 
-// Pass 2a: per chunk of kScanChunk superblock entries, the four sums.
+// Scan 1: per chunk of kScanChunk superblock entries (S digits each), the
+// S sums.
+template <uint32_t S>
 __global__ void __launch_bounds__(256)
-quad_scan_partial_kernel(uint64_t const* __restrict__ sb, uint64_t count,
-                         uint64_t* __restrict__ chunk) {
+group_scan_partial_kernel(uint64_t const* __restrict__ sb, uint64_t count,
+                          uint64_t* __restrict__ chunk) {
   uint64_t const first = uint64_t(blockIdx.x) * kScanChunk;
-  uint64_t c[4] = {0, 0, 0, 0};
+  uint64_t c[S];
+  for (uint32_t d = 0; d < S; ++d) c[d] = 0;
   for (uint64_t i = first + threadIdx.x; i < min(count, first + kScanChunk);
        i += blockDim.x)
-    for (uint32_t d = 0; d < 4; ++d) c[d] += sb[i * 4 + d];
-  for (uint32_t d = 0; d < 4; ++d) {
+    for (uint32_t d = 0; d < S; ++d) c[d] += sb[i * S + d];
+  for (uint32_t d = 0; d < S; ++d) {
     uint64_t tot = 0;
     cta_exclusive_scan(c[d], &tot);
-    if (threadIdx.x == 0) chunk[blockIdx.x * 4 + d] = tot;
+    if (threadIdx.x == 0) chunk[blockIdx.x * S + d] = tot;
   }
 }
 
-// Pass 2b: exclusive prefix of the chunk sums (one thread per digit).
-__global__ void quad_scan_chunks_kernel(uint64_t* __restrict__ chunk,
-                                        uint64_t chunks) {
+// Scan 2: exclusive prefix of the chunk sums (one thread per digit).
+template <uint32_t S>
+__global__ void group_scan_chunks_kernel(uint64_t* __restrict__ chunk,
+                                         uint64_t chunks) {
   uint32_t const d = threadIdx.x;
-  if (d >= 4) return;
+  if (d >= S) return;
   uint64_t run = 0;
   for (uint64_t i = 0; i < chunks; ++i) {
-    uint64_t const x = chunk[i * 4 + d];
-    chunk[i * 4 + d] = run;
+    uint64_t const x = chunk[i * S + d];
+    chunk[i * S + d] = run;
     run += x;
   }
 }
 
-// Pass 2c: exclusive prefix of every entry, in place (1024 threads; two
-// digits packed per 64-bit scan: a round's sums stay below 2^32).
+// Scan 3: exclusive prefix of every entry, in place (1024 threads; two
+// digits packed per 64-bit scan: every entry is below 2^16, a round's sums
+// below 2^32).
+template <uint32_t S>
 __global__ void __launch_bounds__(1024)
-quad_scan_apply_kernel(uint64_t* __restrict__ sb, uint64_t count,
-                       uint64_t const* __restrict__ chunk) {
+group_scan_apply_kernel(uint64_t* __restrict__ sb, uint64_t count,
+                        uint64_t const* __restrict__ chunk) {
   uint64_t const first = uint64_t(blockIdx.x) * kScanChunk;
   uint64_t const end = min(count, first + kScanChunk);
-  uint64_t carry[4];
-  for (uint32_t d = 0; d < 4; ++d) carry[d] = chunk ? chunk[blockIdx.x * 4 + d] : 0;
+  uint64_t carry[S];
+  for (uint32_t d = 0; d < S; ++d) carry[d] = chunk ? chunk[blockIdx.x * S + d] : 0;
   for (uint64_t base = first; base < end; base += blockDim.x) {
     uint64_t const i = base + threadIdx.x;
     bool const in = i < end;
-    uint4 const a = in ? reinterpret_cast<uint4 const*>(sb)[i * 2] : make_uint4(0, 0, 0, 0);
-    uint4 const b = in ? reinterpret_cast<uint4 const*>(sb)[i * 2 + 1] : make_uint4(0, 0, 0, 0);
-    // per entry each digit count is below 2^16 (49,152 digits per superblock)
-    uint64_t tot01 = 0, tot23 = 0;
-    uint64_t const e01 = cta_exclusive_scan(uint64_t(a.x) | (uint64_t(a.z) << 32), &tot01);
-    uint64_t const e23 = cta_exclusive_scan(uint64_t(b.x) | (uint64_t(b.z) << 32), &tot23);
-    if (in) {
-      uint64_t* o = sb + i * 4;
-      o[0] = carry[0] + (e01 & 0xFFFFFFFFu);
-      o[1] = carry[1] + (e01 >> 32);
-      o[2] = carry[2] + (e23 & 0xFFFFFFFFu);
-      o[3] = carry[3] + (e23 >> 32);
+#pragma unroll
+    for (uint32_t k = 0; k < S / 2; ++k) {
+      uint4 const a = in ? reinterpret_cast<uint4 const*>(sb + i * S)[k]
+                         : make_uint4(0, 0, 0, 0);
+      uint64_t tot = 0;
+      uint64_t const e = cta_exclusive_scan(uint64_t(a.x) | (uint64_t(a.z) << 32), &tot);
+      if (in) {
+        sb[i * S + 2 * k] = carry[2 * k] + (e & 0xFFFFFFFFu);
+        sb[i * S + 2 * k + 1] = carry[2 * k + 1] + (e >> 32);
+      }
+      carry[2 * k] += tot & 0xFFFFFFFFu;
+      carry[2 * k + 1] += tot >> 32;
     }
-    carry[0] += tot01 & 0xFFFFFFFFu;
-    carry[1] += tot01 >> 32;
-    carry[2] += tot23 & 0xFFFFFFFFu;
-    carry[3] += tot23 >> 32;
   }
 }
 
+// Counts before every superblock of one level's table (nsb + 1 entries of
+// S digits, the last one zero before and the totals after).
+template <uint32_t S>
+void scan_superblocks(uint64_t* sb, uint64_t entries, DevBuf& chunk, cudaStream_t st) {
+  uint64_t const chunks = ceil_div(entries, kScanChunk);
+  if (chunks > 1) {
+    group_scan_partial_kernel<S><<<static_cast<uint32_t>(chunks), 256, 0, st>>>(
+        sb, entries, chunk.as<uint64_t>());
+    EWT_LAUNCHED();
+    group_scan_chunks_kernel<S><<<1, 32, 0, st>>>(chunk.as<uint64_t>(), chunks);
+    EWT_LAUNCHED();
+  }
+  group_scan_apply_kernel<S><<<static_cast<uint32_t>(chunks), 1024, 0, st>>>(
+      sb, entries, chunks > 1 ? chunk.as<uint64_t>() : nullptr);
+  EWT_LAUNCHED();
+}
+
 // Dense samples of one block: entry k of digit d names the block holding
-// its (k * 2^sh + 1)-th occurrence; before/c = occurrences before / in it.
-__device__ __forceinline__ void put_quad_samples(uint32_t* __restrict__ ds,
-                                                 QuadLevel const& ql, uint32_t sh,
-                                                 uint64_t blk,
-                                                 uint64_t const before[4],
-                                                 uint32_t const c[4]) {
+// its (k * 2^sel_shift + 1)-th occurrence; before/c = occurrences before /
+// in it (S = 2^width digits).
+template <uint32_t S>
+__device__ __forceinline__ void put_group_samples(uint32_t* __restrict__ ds,
+                                                  QuadLevel const& ql, uint64_t blk,
+                                                  uint64_t const before[S],
+                                                  uint32_t const c[S]) {
+  uint32_t const sh = ql.sel_shift;
   uint64_t const R = uint64_t(1) << sh;
 #pragma unroll
-  for (uint32_t d = 0; d < 4; ++d) {
+  for (uint32_t d = 0; d < S; ++d) {
     if (c[d] == 0) continue;
-    // entries fit in 32 bits (at most n / 32 of them)
+    // entries fit in 32 bits (at most n / 16 of them)
     uint32_t const entries = static_cast<uint32_t>((ql.total[d] + R - 1) >> sh);
     uint32_t const last =
         min(static_cast<uint32_t>((before[d] + c[d] - 1) >> sh), entries - 1);
-    uint32_t* S = ds + ql.ds_off[d];
+    uint32_t* S_ = ds + ql.ds_off[d];
     for (uint32_t k = static_cast<uint32_t>((before[d] + R - 1) >> sh); k <= last; ++k)
-      S[k] = static_cast<uint32_t>(blk);
+      S_[k] = static_cast<uint32_t>(blk);
   }
 }
 
@@ -338,14 +376,13 @@ __device__ __forceinline__ uint32_t group_exclusive_scan32(uint32_t x, uint32_t*
 // own superblocks (one thread per 96-digit block), the digit table shared
 // in shared memory.
 __global__ void __launch_bounds__(1024, 1)
-quad_level_kernel(TreeView v, uint32_t j, QuadLevel ql,
+quad_level_kernel(TreeView v, uint32_t l, QuadLevel ql,
                   uint32_t const* __restrict__ hi_w, uint64_t hi_words,
                   uint32_t const* __restrict__ lo_w, uint64_t lo_limit,
                   uint16_t const* __restrict__ lut_g,
                   uint4* __restrict__ blocks, uint64_t const* __restrict__ sb,
                   SbStart const* __restrict__ info, uint64_t nsb,
-                  uint32_t* __restrict__ ds, uint32_t sel_shift,
-                  uint32_t* __restrict__ err) {
+                  uint32_t* __restrict__ ds, uint32_t* __restrict__ err) {
   extern __shared__ __align__(16) uint16_t lut[];
   {
     uint4 const* src = reinterpret_cast<uint4 const*>(lut_g);
@@ -354,7 +391,7 @@ quad_level_kernel(TreeView v, uint32_t j, QuadLevel ql,
   }
   __syncthreads();
   uint64_t const n = v.n;
-  uint32_t const l = 2 * j, sh = v.levels - l;
+  uint32_t const sh = v.levels - l;
   uint64_t const nodes = uint64_t(1) << l;
   uint32_t const t = threadIdx.x & (kQuadSbBlocks - 1);  // block inside its superblock
   // half h of CTA b takes superblocks 2b + h, 2b + h + 2G, ...
@@ -377,7 +414,7 @@ quad_level_kernel(TreeView v, uint32_t j, QuadLevel ql,
       ones += __popc(h[k]);
     }
     uint32_t tot = 0;
-    // ones of level 2j in the superblock before this block (= its digits 2
+    // ones of level l in the superblock before this block (= its digits 2
     // and 3 before it)
     uint32_t const h23 = group_exclusive_scan32(ones, &tot);
     uint64_t r1 = st.rank1 + h23;  // ones before p
@@ -449,60 +486,356 @@ quad_level_kernel(TreeView v, uint32_t j, QuadLevel ql,
     uint4* out = blocks + blk * 2;
     out[0] = make_uint4(h0 | (h1 << 16), h2, dw[0], dw[1]);
     out[1] = make_uint4(dw[2], dw[3], dw[4], dw[5]);
-    if (ds) {
+    if (ds && ql.sel_shift) {
       uint32_t const vb = static_cast<uint32_t>(min(uint64_t(kQuadDigits), n - p));
       uint32_t const c[4] = {vb - ones - c1, c1, ones - c3, c3};
       uint64_t const before[4] = {sbe[0] + h0, sbe[1] + h1, sbe[2] + h2, sbe[3] + h3};
-      put_quad_samples(ds, ql, sel_shift, blk, before, c);
+      put_group_samples<4>(ds, ql, blk, before, c);
     }
   }
 }
 
-// Dense samples of one quad level from its finished blocks (rate changes).
+// Bits q .. q+63 of a bit array with slack behind its end.
+__device__ __forceinline__ uint64_t bits64(uint32_t const* __restrict__ w, uint64_t q) {
+  return uint64_t(bits_fast(w, q)) | (uint64_t(bits_fast(w, q + 32)) << 32);
+}
+
+// Routes two runs into level-l order, eight positions per table lookup:
+// position k takes the next bit of run a1 if bit k of h is set, else the
+// next bit of run a0.  Table entry (hb << 8 | v) holds the 8 routed bits for
+// high byte hb, v = the next 8 - popc(hb) bits of a0 then popc(hb) of a1.
+template <uint32_t kChunks>
+__device__ __forceinline__ uint64_t route_runs(uint8_t const* lut, uint64_t h,
+                                               uint64_t a0, uint64_t a1) {
+  uint64_t out = 0;
+#pragma unroll
+  for (uint32_t i = 0; i < kChunks; ++i) {
+    uint32_t const hb = static_cast<uint32_t>(h >> (8 * i)) & 0xFFu;
+    uint32_t const o = __popc(hb), z = 8 - o;
+    uint32_t const v = (static_cast<uint32_t>(a0) & ((1u << z) - 1u)) |
+                       ((static_cast<uint32_t>(a1) & ((1u << o) - 1u)) << z);
+    a0 >>= z;
+    a1 >>= o;
+    out |= uint64_t(lut[(hb << 8) | v]) << (8 * i);
+  }
+  return out;
+}
+
+void make_route_lut(std::vector<uint8_t>& lut) {
+  lut.assign(65536, 0);
+  for (uint32_t hb = 0; hb < 256; ++hb) {
+    uint32_t const o = static_cast<uint32_t>(__builtin_popcount(hb)), z = 8 - o;
+    for (uint32_t v = 0; v < 256; ++v) {
+      uint32_t r0 = v & ((1u << z) - 1u), r1 = v >> z, out = 0;
+      for (uint32_t k = 0; k < 8; ++k) {
+        uint32_t bit;
+        if (hb >> k & 1u) { bit = r1 & 1u; r1 >>= 1; } else { bit = r0 & 1u; r0 >>= 1; }
+        out |= bit << k;
+      }
+      lut[(hb << 8) | v] = static_cast<uint8_t>(out);
+    }
+  }
+}
+
+// Routed plane bits of positions [p0, pend) of level l (pend - p0 <= 32)
+// whose node may change inside: bit q = the plane's bit at the child
+// position of p0 + q.  h = their level-l bits, r1 = ones of level l before p0.
+__device__ uint32_t route_slow(TreeView const& v, uint32_t l, uint32_t sh,
+                               uint64_t nodes, uint32_t h, uint64_t r1, uint64_t p0,
+                               uint64_t pend, uint32_t const* __restrict__ plane,
+                               uint64_t limit, uint32_t* __restrict__ err) {
+  uint32_t out = 0;
+  uint64_t pos = p0;
+  uint32_t guard = 0;
+  while (pos < pend && guard++ < 32) {
+    QuadNode const nd = quad_node(v, l, sh, nodes, node_of(v.counts, sh, nodes, pos));
+    if (nd.end <= pos) break;  // inconsistent table (reported below)
+    uint64_t const se = min(pend, nd.end);
+    uint32_t const k0 = static_cast<uint32_t>(pos - p0);
+    uint32_t const k1 = static_cast<uint32_t>(se - p0);
+    uint64_t const ob = r1 + __popc(h & ((1u << k0) - 1u)) - nd.ones_before;
+    uint32_t a0 = bits_at(plane, limit, pos - ob);
+    uint32_t a1 = bits_at(plane, limit, nd.start + nd.zeros + ob);
+    for (uint32_t q = k0; q < k1; ++q) {
+      uint32_t bit;
+      if (h >> q & 1u) { bit = a1 & 1u; a1 >>= 1; } else { bit = a0 & 1u; a0 >>= 1; }
+      out |= bit << q;
+    }
+    pos = se;
+  }
+  if (pos < pend) atomicOr(err, 1u);
+  return out;
+}
+
+// Node, ones before and uniformity of every superblock of sb_pos positions
+// of level l (thread per superblock).
+__global__ void __launch_bounds__(128)
+sb_info_kernel(TreeView v, uint32_t l, uint64_t sb_pos, uint64_t nsb,
+               SbStart* __restrict__ info) {
+  uint64_t const s = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (s >= nsb) return;
+  uint64_t const n = v.n;
+  uint64_t const a = s * sb_pos, e = min(n, a + sb_pos);
+  if (a >= e) {
+    info[s] = SbStart{QuadNode{0, n, 0, 0}, 0, 1};
+    return;
+  }
+  uint32_t const sh = v.levels - l;
+  uint64_t const nodes = uint64_t(1) << l;
+  QuadNode const nd = quad_node(v, l, sh, nodes, node_of(v.counts, sh, nodes, a));
+  uint64_t const r1 = ecl::detail::rs_rank1<false>(v.rs, v.rs.meta[l], a, nullptr);
+  info[s] = SbStart{nd, r1, e <= nd.end ? 1u : 0u};
+}
+
+__device__ __forceinline__ void load_lut8(uint8_t* lut, uint8_t const* lut_g) {
+  uint4 const* src = reinterpret_cast<uint4 const*>(lut_g);
+  uint4* dst = reinterpret_cast<uint4*>(lut);
+  for (uint32_t i = threadIdx.x; i < 65536 / 16; i += blockDim.x) dst[i] = src[i];
+  __syncthreads();
+}
+
+// Level l+1's bits routed into level-l order: persistent CTAs of 1024
+// threads, each 512-thread half on its own superblocks, one thread per 64
+// positions (2 output words).
+__global__ void __launch_bounds__(1024, 1)
+merge_plane_kernel(TreeView v, uint32_t l, uint32_t const* __restrict__ hi_w,
+                   uint32_t const* __restrict__ lo_w, uint64_t lo_limit,
+                   uint8_t const* __restrict__ lut_g, SbStart const* __restrict__ info,
+                   uint64_t nsb, uint32_t* __restrict__ out, uint32_t* __restrict__ err) {
+  extern __shared__ __align__(16) uint8_t lut8[];
+  load_lut8(lut8, lut_g);
+  uint64_t const n = v.n;
+  uint32_t const sh = v.levels - l;
+  uint64_t const nodes = uint64_t(1) << l;
+  uint32_t const t = threadIdx.x & 511;
+  uint64_t const first = uint64_t(blockIdx.x) * 2 + (threadIdx.x >> 9);
+  for (uint64_t sbi = first; sbi < nsb; sbi += uint64_t(gridDim.x) * 2) {
+    SbStart const st = info[sbi];
+    uint64_t const p = (sbi * 512 + t) * 64;
+    uint32_t const valid = p < n ? static_cast<uint32_t>(min(uint64_t(64), n - p)) : 0u;
+    uint64_t const vm = valid == 64 ? ~0ull : (1ull << valid) - 1;
+    uint64_t const wi = p >> 5;
+    uint64_t const h =
+        valid ? (uint64_t(hi_w[wi]) | (uint64_t(hi_w[wi + 1]) << 32)) & vm : 0ull;
+    uint32_t tot = 0;
+    uint64_t const r1 = st.rank1 + group_exclusive_scan32(__popcll(h), &tot);
+    if (!valid) continue;
+    uint64_t m;
+    if (st.uniform) {
+      uint64_t const ob = r1 - st.node.ones_before;  // node ones before p
+      m = route_runs<8>(lut8, h, bits64(lo_w, p - ob),
+                        bits64(lo_w, st.node.start + st.node.zeros + ob));
+    } else {
+      uint64_t const e0 = min(n, p + 32);
+      m = route_slow(v, l, sh, nodes, static_cast<uint32_t>(h), r1, p, e0, lo_w,
+                     lo_limit, err);
+      if (valid > 32)
+        m |= uint64_t(route_slow(v, l, sh, nodes, static_cast<uint32_t>(h >> 32),
+                                 r1 + __popc(static_cast<uint32_t>(h)), p + 32,
+                                 min(n, p + 64), lo_w, lo_limit, err))
+             << 32;
+    }
+    m &= vm;
+    out[wi] = static_cast<uint32_t>(m);
+    out[wi + 1] = static_cast<uint32_t>(m >> 32);
+  }
+}
+
+// Bits k of x (k < 21) to bits 3k.
+__device__ __forceinline__ uint64_t spread3(uint64_t x) {
+  x &= 0x1FFFFFull;
+  x = (x | (x << 32)) & 0x1F00000000FFFFull;
+  x = (x | (x << 16)) & 0x1F0000FF0000FFull;
+  x = (x | (x << 8)) & 0x100F00F00F00F00Full;
+  x = (x | (x << 4)) & 0x10C30C30C30C30C3ull;
+  x = (x | (x << 2)) & 0x1249249249249249ull;
+  return x;
+}
+
+// Exclusive scan of four uint32 over one 512-thread half (as
+// group_exclusive_scan32, one set of barriers).
+__device__ __forceinline__ uint4 group_exclusive_scan4(uint4 x, uint4* total) {
+  __shared__ uint4 ws4[2][16];
+  uint32_t const lane = threadIdx.x & 31, wid = (threadIdx.x >> 5) & 15;
+  uint32_t const g = threadIdx.x >> 9;
+  uint4* const ws = ws4[g];
+  uint4 inc = x;
+#pragma unroll
+  for (uint32_t o = 1; o < 32; o <<= 1) {
+    uint32_t const a = __shfl_up_sync(0xFFFFFFFFu, inc.x, o);
+    uint32_t const b = __shfl_up_sync(0xFFFFFFFFu, inc.y, o);
+    uint32_t const c = __shfl_up_sync(0xFFFFFFFFu, inc.z, o);
+    uint32_t const d = __shfl_up_sync(0xFFFFFFFFu, inc.w, o);
+    if (lane >= o) { inc.x += a; inc.y += b; inc.z += c; inc.w += d; }
+  }
+  if (lane == 31) ws[wid] = inc;
+  asm volatile("bar.sync %0, 512;" ::"r"(g + 1) : "memory");
+  if (wid == 0) {
+    uint4 t = lane < 16 ? ws[lane] : make_uint4(0, 0, 0, 0);
+#pragma unroll
+    for (uint32_t o = 1; o < 16; o <<= 1) {
+      uint32_t const a = __shfl_up_sync(0xFFFFFFFFu, t.x, o);
+      uint32_t const b = __shfl_up_sync(0xFFFFFFFFu, t.y, o);
+      uint32_t const c = __shfl_up_sync(0xFFFFFFFFu, t.z, o);
+      uint32_t const d = __shfl_up_sync(0xFFFFFFFFu, t.w, o);
+      if (lane >= o) { t.x += a; t.y += b; t.z += c; t.w += d; }
+    }
+    if (lane < 16) ws[lane] = t;
+  }
+  asm volatile("bar.sync %0, 512;" ::"r"(g + 1) : "memory");
+  uint4 const before = wid ? ws[wid - 1] : make_uint4(0, 0, 0, 0);
+  *total = ws[15];
+  asm volatile("bar.sync %0, 512;" ::"r"(g + 1) : "memory");
+  return make_uint4(before.x + inc.x - x.x, before.y + inc.y - x.y,
+                    before.z + inc.z - x.z, before.w + inc.w - x.w);
+}
+
+// Octal level at l: one thread per 42-digit block, each 512-thread half on
+// its own superblocks.  Digit = (level l bit, level l+1 routed, plane routed)
+// with the plane = level l+2 in level-(l+1) order.  Writes the blocks and the
+// superblock's digit counts (scanned afterwards).
+__global__ void __launch_bounds__(1024, 1)
+octal_level_kernel(TreeView v, uint32_t l, uint32_t const* __restrict__ hi_w,
+                   uint32_t const* __restrict__ mid_w, uint64_t mid_limit,
+                   uint32_t const* __restrict__ low_w, uint64_t low_limit,
+                   uint8_t const* __restrict__ lut_g, SbStart const* __restrict__ info,
+                   uint64_t nsb, uint64_t num_blocks, uint4* __restrict__ blocks,
+                   uint64_t* __restrict__ sb, uint32_t* __restrict__ err) {
+  extern __shared__ __align__(16) uint8_t lut8[];
+  load_lut8(lut8, lut_g);
+  uint64_t const n = v.n;
+  uint32_t const sh = v.levels - l;
+  uint64_t const nodes = uint64_t(1) << l;
+  uint32_t const t = threadIdx.x & (kOctSbBlocks - 1);
+  uint64_t const first = uint64_t(blockIdx.x) * 2 + (threadIdx.x >> 9);
+  for (uint64_t sbi = first; sbi < nsb; sbi += uint64_t(gridDim.x) * 2) {
+    SbStart const st = info[sbi];
+    uint64_t const blk = sbi * kOctSbBlocks + t;
+    bool const mine = blk < num_blocks;
+    uint64_t const p = blk * kOctDigits;
+    uint32_t const valid =
+        mine && p < n ? static_cast<uint32_t>(min(uint64_t(kOctDigits), n - p)) : 0u;
+    uint64_t const vm = (1ull << valid) - 1;  // valid <= 42
+    uint64_t const H = valid ? bits64(hi_w, p) & vm : 0ull;
+    uint32_t tot = 0;
+    uint64_t const r1 = st.rank1 + group_exclusive_scan32(__popcll(H), &tot);
+    uint64_t M = 0, B = 0;
+    if (valid) {
+      if (st.uniform) {
+        uint64_t const ob = r1 - st.node.ones_before;
+        uint64_t const q0 = p - ob, q1 = st.node.start + st.node.zeros + ob;
+        M = route_runs<6>(lut8, H, bits64(mid_w, q0), bits64(mid_w, q1)) & vm;
+        B = route_runs<6>(lut8, H, bits64(low_w, q0), bits64(low_w, q1)) & vm;
+      } else {
+        uint64_t const end = p + valid;
+#pragma unroll
+        for (uint32_t k = 0; k < 2; ++k) {
+          uint64_t const p0 = p + 32 * k;
+          if (p0 >= end) break;
+          uint64_t const pe = min(end, p0 + 32);
+          uint32_t const hk = static_cast<uint32_t>(H >> (32 * k));
+          uint64_t const rk = r1 + (k ? __popc(static_cast<uint32_t>(H)) : 0u);
+          M |= uint64_t(route_slow(v, l, sh, nodes, hk, rk, p0, pe, mid_w, mid_limit, err))
+               << (32 * k);
+          B |= uint64_t(route_slow(v, l, sh, nodes, hk, rk, p0, pe, low_w, low_limit, err))
+               << (32 * k);
+        }
+      }
+    }
+    uint32_t c[8];
+#pragma unroll
+    for (uint32_t d = 0; d < 8; ++d)
+      c[d] = __popcll((d & 4 ? H : ~H) & (d & 2 ? M : ~M) & (d & 1 ? B : ~B) & vm);
+    uint4 tot4;
+    // every count below 2^16 (21,504 digits per superblock): two per word
+    uint4 const e = group_exclusive_scan4(
+        make_uint4(c[0] | (c[1] << 16), c[2] | (c[3] << 16), c[4] | (c[5] << 16),
+                   c[6] | (c[7] << 16)),
+        &tot4);
+    if (t == 0) {
+      uint64_t* o = sb + sbi * 8;
+      uint32_t const w4[4] = {tot4.x, tot4.y, tot4.z, tot4.w};
+#pragma unroll
+      for (uint32_t d = 0; d < 8; ++d) o[d] = (w4[d >> 1] >> (16 * (d & 1))) & 0xFFFFu;
+    }
+    if (!mine) continue;
+    uint64_t const w2 = (spread3(H) << 2) | (spread3(M) << 1) | spread3(B);
+    uint64_t const w3 = (spread3(H >> 21) << 2) | (spread3(M >> 21) << 1) | spread3(B >> 21);
+    uint4* out = blocks + blk * 2;
+    out[0] = make_uint4(e.x, e.y, e.z, e.w & 0xFFFFu);
+    out[1] = make_uint4(static_cast<uint32_t>(w2), static_cast<uint32_t>(w2 >> 32),
+                        static_cast<uint32_t>(w3), static_cast<uint32_t>(w3 >> 32));
+  }
+}
+
+// Dense samples of one group level from its finished blocks and scanned
+// superblock table; block 0 also checks the level's digit totals.
+template <int W>
 __global__ void __launch_bounds__(256)
-quad_samples_kernel(uint4 const* __restrict__ blocks,
-                    uint64_t const* __restrict__ sb, uint64_t n, QuadLevel ql,
-                    uint32_t* __restrict__ ds, uint32_t sh) {
+group_samples_kernel(uint4 const* __restrict__ blocks, uint64_t const* __restrict__ sb,
+                     uint64_t n, QuadLevel ql, uint32_t* __restrict__ ds,
+                     uint32_t* __restrict__ err) {
+  constexpr uint32_t S = 1u << W;
+  constexpr uint32_t kD = GroupShape<W>::kDigits, kSb = GroupShape<W>::kSbBlocks;
   uint64_t const b = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
-  if (b >= ql.num_blocks) return;
+  if (b == 0 && err) {
+    uint64_t const* tot = sb + (ql.num_blocks + kSb - 1) / kSb * S;
+    for (uint32_t d = 0; d < S; ++d)
+      if (tot[d] != ql.total[d]) atomicOr(err, 4u);
+  }
+  if (!ds || ql.sel_shift == 0 || b >= ql.num_blocks) return;
   uint4 const x = blocks[b * 2], y = blocks[b * 2 + 1];
   uint64_t q[4];
   ecl::detail::quad_words(x, y, q);
-  uint64_t const first = b * kQuadDigits;
-  uint32_t const valid =
-      first < n ? static_cast<uint32_t>(min(uint64_t(kQuadDigits), n - first)) : 0u;
-  uint64_t const* sbv = sb + (b / kQuadSbBlocks) * 4;
-  uint64_t before[4];
-  uint32_t c[4];
+  uint64_t const first = b * kD;
+  uint32_t const valid = first < n ? static_cast<uint32_t>(min(uint64_t(kD), n - first)) : 0u;
+  uint64_t const* sbv = sb + (b / kSb) * S;
+  uint64_t before[S];
+  uint32_t c[S];
 #pragma unroll
-  for (uint32_t d = 0; d < 4; ++d) {
-    c[d] = ecl::detail::quad_count(q, d, valid);
-    before[d] = ecl::detail::quad_before(q[0], sbv[d], d, b);
+  for (uint32_t d = 0; d < S; ++d) {
+    c[d] = ecl::detail::group_count<W>(q, d, valid);
+    before[d] = ecl::detail::group_before<W>(q[0], q[1], sbv[d], d, b);
   }
-  put_quad_samples(ds, ql, sh, b, before, c);
+  put_group_samples<S>(ds, ql, b, before, c);
 }
 
-// Lays out the dense samples of every quad level at rate 2^shift.
+// Sample shift of a group level for the tree-wide rate 2^shift: octal
+// digits are about half as frequent and blocks hold 42 instead of 96, so
+// octal levels sample 4 times as densely (same blocks per bracket).
+uint32_t level_shift(uint32_t width, uint32_t shift) {
+  if (shift == 0) return 0;
+  return width == 3 ? std::max<uint32_t>(shift, 6) - 2 : shift;
+}
+
+// Lays out the dense samples of every group level at rate 2^shift.
 void layout_quad_samples(QuadStore& qs, uint32_t shift) {
   qs.ds.reset();
   qs.sel_shift = shift;
-  if (shift == 0) return;
   uint64_t total = 0;
-  for (auto& ql : qs.levels)
-    for (uint32_t d = 0; d < 4; ++d) {
+  for (auto& ql : qs.levels) {
+    ql.sel_shift = level_shift(ql.width, shift);
+    for (uint32_t d = 0; d < 8; ++d) ql.ds_off[d] = 0;
+    if (!ql.sel_shift) continue;
+    for (uint32_t d = 0; d < (1u << ql.width); ++d) {
       ql.ds_off[d] = total;
-      total += ceil_div(ql.total[d], uint64_t(1) << shift);
+      total += ceil_div(ql.total[d], uint64_t(1) << ql.sel_shift);
     }
-  qs.ds.alloc(std::max<uint64_t>(total, 1) * 4);
+  }
+  if (shift) qs.ds.alloc(std::max<uint64_t>(total, 1) * 4);
 }
 
-void run_quad_samples(QuadStore& qs, uint64_t n, cudaStream_t st) {
-  if (!qs.ds.get() || qs.sel_shift == 0) return;
+void run_quad_samples(QuadStore& qs, uint64_t n, uint32_t* err, cudaStream_t st) {
+  if (!qs.ds.get()) return;
   for (auto const& ql : qs.levels) {
-    quad_samples_kernel<<<static_cast<uint32_t>(ceil_div(ql.num_blocks, 256)), 256, 0,
-                          st>>>(qs.blocks.as<uint4>() + ql.blk_off * 2,
-                                qs.sb.as<uint64_t>() + ql.sb_off * 4, n, ql,
-                                qs.ds.as<uint32_t>(), qs.sel_shift);
+    uint32_t* const ds = qs.ds.get() ? qs.ds.as<uint32_t>() : nullptr;
+    uint32_t const grid = static_cast<uint32_t>(ceil_div(ql.num_blocks, 256));
+    uint4 const* const blocks = qs.blocks.as<uint4>() + ql.blk_off * 2;
+    uint64_t const* const sb = qs.sb.as<uint64_t>() + ql.sb_off;
+    if (ql.width == 3)
+      group_samples_kernel<3><<<grid, 256, 0, st>>>(blocks, sb, n, ql, ds, err);
+    else
+      group_samples_kernel<2><<<grid, 256, 0, st>>>(blocks, sb, n, ql, ds, err);
     EWT_LAUNCHED();
   }
 }
@@ -517,6 +850,15 @@ void upload_levels(QuadStore& qs, cudaStream_t st) {
 
 }  // namespace
 
+std::vector<uint32_t> group_widths(uint32_t L) {
+  std::vector<uint32_t> w;
+  if (L < 2) return w;
+  uint32_t const quads = L % 3 == 0 ? 0 : L % 3 == 2 ? 1 : 2;
+  for (uint32_t i = 0; i < (L - 2 * quads) / 3; ++i) w.push_back(3);
+  for (uint32_t i = 0; i < quads; ++i) w.push_back(2);
+  return w;
+}
+
 QuadView QuadStore::view() const {
   QuadView v{};
   if (levels.empty() || !blocks.get()) return v;
@@ -526,7 +868,9 @@ QuadView QuadStore::view() const {
   v.node_ranks = node_ranks.as<uint64_t>();
   v.levels = levels_d.as<QuadLevel>();
   v.num = static_cast<uint32_t>(levels.size());
-  v.sel_shift = v.ds ? sel_shift : 0;
+  uint32_t covered = 0;
+  for (auto const& ql : levels) covered += ql.width;
+  v.covered = covered;
   return v;
 }
 
@@ -538,36 +882,51 @@ void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, cudaStream_t st) {
   qs.blocks.reset();
   if (!quad_eligible(t)) return;
   PhaseTimer pt(EWT_PHASE_QUAD, st);
-  uint32_t const L = t.L, QL = L / 2;
+  uint32_t const L = t.L;
   uint64_t const n = t.n;
   EWT_REQUIRE(C.size() == t.sigma + 1 && C[t.sigma] == n, EWT_ERR_CUDA,
               "count table inconsistent");
+  std::vector<uint32_t> const widths = group_widths(L);
   // host: layout, digit totals, node ranks
   std::vector<uint64_t> nr;
-  uint64_t blk = 0, sbs = 0;
-  qs.levels.resize(QL);
-  for (uint32_t j = 0; j < QL; ++j) {
+  uint64_t blk = 0, sbw = 0, max_info = 0;
+  bool any_octal = false;
+  qs.levels.resize(widths.size());
+  uint32_t l = 0;
+  for (size_t j = 0; j < widths.size(); ++j) {
+    uint32_t const w = widths[j], S = 1u << w;
     QuadLevel& ql = qs.levels[j];
     ql = QuadLevel{};
-    ql.num_blocks = n / kQuadDigits + 1;
+    ql.width = w;
+    ql.start = l;
+    uint32_t const kD = w == 3 ? kOctDigits : kQuadDigits;
+    uint32_t const kSb = w == 3 ? kOctSbBlocks : kQuadSbBlocks;
+    ql.num_blocks = n / kD + 1;
     ql.blk_off = blk;
-    ql.sb_off = sbs;
+    ql.sb_off = sbw;
     ql.nr_off = nr.size();
     blk += ql.num_blocks;
-    sbs += ceil_div(ql.num_blocks, kQuadSbBlocks) + 1;  // + the totals entry
-    uint32_t const sh = L - 2 * j;  // symbols under a level-2j node: 2^sh
-    uint64_t const nodes = uint64_t(1) << (2 * j);
-    uint64_t run[4] = {0, 0, 0, 0};
+    uint64_t const nsb = ceil_div(ql.num_blocks, uint64_t(kSb));
+    sbw += (nsb + 1) * S;  // + the totals entry
+    max_info = std::max(max_info, nsb);
+    if (w == 3) {
+      any_octal = true;
+      max_info = std::max(max_info, ceil_div(n, kMergeSbPos));
+    }
+    uint32_t const sh = L - l;  // symbols under a level-l node: 2^sh
+    uint64_t const nodes = uint64_t(1) << l;
+    uint64_t run[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (uint64_t g = 0; g < nodes; ++g)
-      for (uint32_t d = 0; d < 4; ++d) {
+      for (uint32_t d = 0; d < S; ++d) {
         nr.push_back(run[d]);
-        uint64_t const pre = (g << 2) | d;  // prefix of 2j + 2 bits
-        run[d] += C[(pre + 1) << (sh - 2)] - C[pre << (sh - 2)];
+        uint64_t const pre = (g << w) | d;  // prefix of l + w bits
+        run[d] += C[(pre + 1) << (sh - w)] - C[pre << (sh - w)];
       }
-    for (uint32_t d = 0; d < 4; ++d) ql.total[d] = run[d];
+    for (uint32_t d = 0; d < S; ++d) ql.total[d] = run[d];
+    l += w;
   }
   qs.blocks.alloc(blk * 32);
-  qs.sb.alloc(sbs * 32);
+  qs.sb.alloc(sbw * 8);
   qs.node_ranks.alloc(nr.size() * 8);
   EWT_CUDA(cudaMemcpyAsync(qs.node_ranks.get(), nr.data(), nr.size() * 8,
                            cudaMemcpyHostToDevice, st));
@@ -578,51 +937,104 @@ void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, cudaStream_t st) {
     make_digit_lut(v);
     return v;
   }();
-  DevBuf lut_d(lut.size() * 2), err_d(4);
-  EWT_CUDA(cudaMemcpyAsync(lut_d.get(), lut.data(), lut.size() * 2,
-                           cudaMemcpyHostToDevice, st));
+  static std::vector<uint8_t> const lut8 = [] {
+    std::vector<uint8_t> v;
+    make_route_lut(v);
+    return v;
+  }();
+  DevBuf lut_d, lut8_d, plane, err_d(4);
   EWT_CUDA(cudaMemsetAsync(err_d.get(), 0, 4, st));
-  set_smem_limit(quad_level_kernel, 65536 * 2);
-  uint64_t const max_nsb = ceil_div(n / kQuadDigits + 1, kQuadSbBlocks);
-  DevBuf chunk(ceil_div(max_nsb + 1, kScanChunk) * 32);
-  DevBuf info(max_nsb * sizeof(SbStart));
+  uint64_t plane_words = 0;
+  if (any_octal) {
+    lut8_d.alloc(lut8.size());
+    EWT_CUDA(cudaMemcpyAsync(lut8_d.get(), lut8.data(), lut8.size(),
+                             cudaMemcpyHostToDevice, st));
+    plane_words = ceil_div(n, 64) * 2 + 16;  // slack for the 64-bit reads
+    plane.alloc(plane_words * 4);
+    set_smem_limit(merge_plane_kernel, 65536);
+    set_smem_limit(octal_level_kernel, 65536);
+  }
+  if (widths.back() == 2) {
+    lut_d.alloc(lut.size() * 2);
+    EWT_CUDA(cudaMemcpyAsync(lut_d.get(), lut.data(), lut.size() * 2,
+                             cudaMemcpyHostToDevice, st));
+    set_smem_limit(quad_level_kernel, 65536 * 2);
+  }
+  DevBuf chunk(ceil_div(max_info + 1, kScanChunk) * 8 * 8);
+  DevBuf info(std::max<uint64_t>(max_info, 1) * sizeof(SbStart));
   TreeView const& v = t.view;
   uint32_t* const words = t.rs.words.as<uint32_t>();
-  for (uint32_t j = 0; j < QL; ++j) {
-    QuadLevel const& ql = qs.levels[j];
-    ArrayMeta const& mh = t.rs.meta[2 * j];
-    ArrayMeta const& ml = t.rs.meta[2 * j + 1];
-    uint64_t const nsb = ceil_div(ql.num_blocks, kQuadSbBlocks);
-    uint64_t* const sb = qs.sb.as<uint64_t>() + ql.sb_off * 4;
-    quad_sb_count_kernel<<<static_cast<uint32_t>(ceil_div(nsb + 1, 128)), 128, 0, st>>>(
-        v, j, nsb, sb, info.as<SbStart>());
-    EWT_LAUNCHED();
-    uint64_t const chunks = ceil_div(nsb + 1, kScanChunk);
-    if (chunks > 1) {
-      quad_scan_partial_kernel<<<static_cast<uint32_t>(chunks), 256, 0, st>>>(
-          sb, nsb + 1, chunk.as<uint64_t>());
+  uint64_t const total_words = t.rs.total_words;
+  uint32_t const sms = static_cast<uint32_t>(sm_count());
+  for (auto const& ql : qs.levels) {
+    uint32_t const lv = ql.start;
+    ArrayMeta const& m0 = t.rs.meta[lv];
+    ArrayMeta const& m1 = t.rs.meta[lv + 1];
+    uint64_t* const sb = qs.sb.as<uint64_t>() + ql.sb_off;
+    uint4* const blocks = qs.blocks.as<uint4>() + ql.blk_off * 2;
+    if (ql.width == 2) {
+      uint64_t const nsb = ceil_div(ql.num_blocks, uint64_t(kQuadSbBlocks));
+      quad_sb_count_kernel<<<static_cast<uint32_t>(ceil_div(nsb + 1, 128)), 128, 0, st>>>(
+          v, lv, nsb, sb, info.as<SbStart>());
       EWT_LAUNCHED();
-      quad_scan_chunks_kernel<<<1, 32, 0, st>>>(chunk.as<uint64_t>(), chunks);
+      scan_superblocks<4>(sb, nsb + 1, chunk, st);
+      uint32_t const grid =
+          static_cast<uint32_t>(std::min<uint64_t>(ceil_div(nsb, 2), uint64_t(sms)));
+      quad_level_kernel<<<grid, 1024, 65536 * 2, st>>>(
+          v, lv, ql, words + m0.word_off, ceil_div(n, 32), words + m1.word_off,
+          total_words - m1.word_off, lut_d.as<uint16_t>(), blocks, sb,
+          info.as<SbStart>(), nsb, qs.ds.get() ? qs.ds.as<uint32_t>() : nullptr,
+          err_d.as<uint32_t>());
       EWT_LAUNCHED();
+      continue;
     }
-    quad_scan_apply_kernel<<<static_cast<uint32_t>(chunks), 1024, 0, st>>>(
-        sb, nsb + 1, chunks > 1 ? chunk.as<uint64_t>() : nullptr);
+    // octal: level lv+2 routed into level-(lv+1) order first
+    ArrayMeta const& m2 = t.rs.meta[lv + 2];
+    uint64_t const nsb_m = ceil_div(n, kMergeSbPos);
+    sb_info_kernel<<<static_cast<uint32_t>(ceil_div(nsb_m, 128)), 128, 0, st>>>(
+        v, lv + 1, kMergeSbPos, nsb_m, info.as<SbStart>());
     EWT_LAUNCHED();
-    uint32_t const grid = static_cast<uint32_t>(
-        std::min<uint64_t>(ceil_div(nsb, 2), uint64_t(sm_count())));
-    quad_level_kernel<<<grid, 1024, 65536 * 2, st>>>(
-        v, j, ql, words + mh.word_off, ceil_div(n, 32), words + ml.word_off,
-        t.rs.total_words - ml.word_off, lut_d.as<uint16_t>(),
-        qs.blocks.as<uint4>() + ql.blk_off * 2, sb, info.as<SbStart>(), nsb,
-        qs.ds.get() ? qs.ds.as<uint32_t>() : nullptr, qs.sel_shift,
+    merge_plane_kernel<<<static_cast<uint32_t>(
+                             std::min<uint64_t>(ceil_div(nsb_m, 2), uint64_t(sms))),
+                         1024, 65536, st>>>(
+        v, lv + 1, words + m1.word_off, words + m2.word_off, total_words - m2.word_off,
+        lut8_d.as<uint8_t>(), info.as<SbStart>(), nsb_m, plane.as<uint32_t>(),
         err_d.as<uint32_t>());
+    EWT_LAUNCHED();
+    uint64_t const nsb = ceil_div(ql.num_blocks, uint64_t(kOctSbBlocks));
+    sb_info_kernel<<<static_cast<uint32_t>(ceil_div(nsb, 128)), 128, 0, st>>>(
+        v, lv, kOctSbDigits, nsb, info.as<SbStart>());
+    EWT_LAUNCHED();
+    EWT_CUDA(cudaMemsetAsync(sb + nsb * 8, 0, 64, st));  // the totals entry
+    octal_level_kernel<<<static_cast<uint32_t>(
+                             std::min<uint64_t>(ceil_div(nsb, 2), uint64_t(sms))),
+                         1024, 65536, st>>>(
+        v, lv, words + m0.word_off, words + m1.word_off, total_words - m1.word_off,
+        plane.as<uint32_t>(), plane_words, lut8_d.as<uint8_t>(), info.as<SbStart>(), nsb,
+        ql.num_blocks, blocks, sb, err_d.as<uint32_t>());
+    EWT_LAUNCHED();
+    scan_superblocks<8>(sb, nsb + 1, chunk, st);
+  }
+  // octal samples (quad levels wrote theirs) and every level's totals check
+  for (auto const& ql : qs.levels) {
+    uint32_t* const ds = ql.width == 3 && qs.ds.get() ? qs.ds.as<uint32_t>() : nullptr;
+    uint32_t const grid =
+        ds ? static_cast<uint32_t>(ceil_div(ql.num_blocks, 256)) : 1u;
+    uint4 const* const blocks = qs.blocks.as<uint4>() + ql.blk_off * 2;
+    uint64_t const* const sb = qs.sb.as<uint64_t>() + ql.sb_off;
+    if (ql.width == 3)
+      group_samples_kernel<3><<<grid, 256, 0, st>>>(blocks, sb, n, ql, ds,
+                                                    err_d.as<uint32_t>());
+    else
+      group_samples_kernel<2><<<grid, 256, 0, st>>>(blocks, sb, n, ql, ds,
+                                                    err_d.as<uint32_t>());
     EWT_LAUNCHED();
   }
   uint32_t bad = 0;
   EWT_CUDA(cudaMemcpyAsync(&bad, err_d.get(), 4, cudaMemcpyDeviceToHost, st));
   EWT_CUDA(cudaStreamSynchronize(st));
   EWT_REQUIRE(bad == 0, EWT_ERR_CUDA,
-              "internal consistency check failed (quad levels, kind " +
+              "internal consistency check failed (group levels, kind " +
                   std::to_string(bad) + ")");
 }
 
@@ -639,7 +1051,7 @@ void build_quad_samples(ewt_tree& t, uint32_t shift, cudaStream_t st) {
   EWT_CUDA(cudaStreamSynchronize(st));  // no query may read the old samples
   layout_quad_samples(qs, shift);
   upload_levels(qs, st);
-  run_quad_samples(qs, t.n, st);
+  run_quad_samples(qs, t.n, nullptr, st);
   EWT_CUDA(cudaStreamSynchronize(st));
 }
 

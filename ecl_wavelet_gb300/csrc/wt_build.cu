@@ -848,10 +848,13 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
     }
   }
   build_rs_samples(t.rs, st);
-  // binary levels that quad levels cover get no rank blocks
+  // binary levels that group levels cover get no rank blocks
   t.rs.skip_blocks.assign(L, 0);
-  if (quad_eligible(t))
-    for (uint32_t l = 0; l < (L & ~1u); ++l) t.rs.skip_blocks[l] = 1;
+  if (quad_eligible(t)) {
+    uint32_t covered = 0;
+    for (uint32_t w : group_widths(L)) covered += w;
+    for (uint32_t l = 0; l < covered; ++l) t.rs.skip_blocks[l] = 1;
+  }
   build_rank_blocks(t.rs, st);
   v.rs = t.rs.view();
   v.quad = ecl::detail::QuadView{};

@@ -88,28 +88,44 @@ struct RSView {
   uint32_t sel_shift;     // log2 of the dense sample rate; 0 = none
 };
 
-/* Quad (4-ary) query index of power-of-two alphabets (query side, no
- * reference counterpart).  Quad level j pairs binary levels 2j and 2j+1: in
- * level-2j order it holds each symbol's 2-bit digit (bit 2j as the high bit,
- * bit 2j+1 as the low bit, counted from the top), so one read resolves two
- * binary levels.  Storage: 32-byte blocks of 96 digits; bits 0..47 of a
- * block hold the counts of digits 0, 1, 2 since the start of its superblock
- * (512 blocks = 49,152 digits) as uint16, bits 64..255 the digits (digit t
- * at bit 64 + 2t); a superblock table holds the four digit counts before
- * every superblock (uint64).  Dense select samples per digit name the block
- * holding every R-th occurrence (uint32).  node_ranks[j][g][d] = occurrences
- * of digit d before node g of level 2j. */
-constexpr uint32_t kQuadDigits = 96;
-constexpr uint32_t kQuadSbBlocks = 512;
+/* Group levels of power-of-two alphabets (query side, no reference
+ * counterpart).  A group level covers w = 2 or 3 consecutive binary levels
+ * starting at level l: in level-l order it holds each symbol's w-bit digit
+ * (bits l .. l+w-1 counted from the top), so one read resolves w binary
+ * levels.  Storage: 32-byte blocks; a block holds, before its digits, the
+ * counts of digits 0 .. 2^w - 2 since the start of its superblock (uint16;
+ * the last digit's follows), and a superblock table holds the 2^w digit
+ * counts before every superblock (uint64).
+ *   w = 2 (quad): bits 0..47 counts, bits 64..255 96 digits (digit t at bit
+ *         64 + 2t), 512 blocks per superblock (49,152 digits);
+ *   w = 3 (octal): bits 0..111 counts, two 64-bit words of 21 digits each
+ *         (digit t at bit 3 (t mod 21) of word 2 + t / 21), 512 blocks per
+ *         superblock (21,504 digits).
+ * Dense select samples per digit name the block holding every R-th
+ * occurrence (uint32); node_ranks[group][node][digit] = occurrences of the
+ * digit before the node. */
+template <int W> struct GroupShape;
+template <> struct GroupShape<2> {
+  static constexpr uint32_t kDigits = 96, kSbBlocks = 512;
+};
+template <> struct GroupShape<3> {
+  static constexpr uint32_t kDigits = 42, kSbBlocks = 512;
+};
+constexpr uint32_t kQuadDigits = GroupShape<2>::kDigits;
+constexpr uint32_t kQuadSbBlocks = GroupShape<2>::kSbBlocks;
 constexpr uint64_t kQuadSbDigits = uint64_t(kQuadDigits) * kQuadSbBlocks;
 
 struct QuadLevel {
   uint64_t blk_off;     // first block (2 uint4 each)
-  uint64_t sb_off;      // first superblock entry (4 uint64 each)
-  uint64_t ds_off[4];   // first dense sample of each digit
-  uint64_t total[4];    // occurrences of each digit
-  uint64_t nr_off;      // first node-rank entry (4 uint64 per node)
-  uint64_t num_blocks;  // n / 96 + 1 (position n is addressable)
+  uint64_t sb_off;      // first superblock-table word (2^width per superblock)
+  uint64_t ds_off[8];   // first dense sample of each digit
+  uint64_t total[8];    // occurrences of each digit
+  uint64_t nr_off;      // first node-rank entry (2^width per node)
+  uint64_t num_blocks;  // n / digits-per-block + 1 (position n is addressable)
+  uint32_t width;       // digit bits: 2 or 3
+  uint32_t start;       // first binary level of the group
+  uint32_t sel_shift;   // log2 of its dense sample rate (0: no samples)
+  uint32_t reserved;
 };
 
 struct QuadView {
@@ -118,8 +134,8 @@ struct QuadView {
   const uint32_t* ds;          // null: select searches the superblocks
   const uint64_t* node_ranks;
   const QuadLevel* levels;     // device array of num entries
-  uint32_t num;                // quad levels (0: the tree has none)
-  uint32_t sel_shift;          // log2 of the dense sample rate
+  uint32_t num;                // group levels (0: the tree has none)
+  uint32_t covered;            // binary levels they cover (the rest: binary)
 };
 
 /* Everything a query walk needs; trivially copyable into a kernel. */
@@ -392,7 +408,7 @@ __device__ __forceinline__ uint64_t rs_select(const RSView& v,
   return m.bits;  // not reached for valid structures
 }
 
-/* ---- quad levels ------------------------------------------------------ */
+/* ---- group levels ----------------------------------------------------- */
 
 __device__ __forceinline__ void quad_words(uint4 a, uint4 b, uint64_t q[4]) {
   q[0] = (uint64_t(a.y) << 32) | a.x;
@@ -401,167 +417,215 @@ __device__ __forceinline__ void quad_words(uint4 a, uint4 b, uint64_t q[4]) {
   q[3] = (uint64_t(b.w) << 32) | b.z;
 }
 
-/* Bit 2k of the result is set iff 2-bit lane k of q equals d. */
-__device__ __forceinline__ uint64_t quad_match(uint64_t q, uint32_t d) {
-  uint64_t const e = ~(q ^ (0x5555555555555555ull * d));
-  return e & (e >> 1) & 0x5555555555555555ull;
+/* Lane-match masks: the lowest bit of every W-bit lane of q equal to d. */
+template <int W>
+__device__ __forceinline__ uint64_t group_match(uint64_t q, uint32_t d) {
+  if constexpr (W == 2) {
+    uint64_t const e = ~(q ^ (0x5555555555555555ull * d));
+    return e & (e >> 1) & 0x5555555555555555ull;
+  } else {
+    constexpr uint64_t kLanes = 0x1249249249249249ull & ((1ull << 63) - 1);  // 21 lanes
+    uint64_t const e = ~(q ^ (kLanes * d));
+    return e & (e >> 1) & (e >> 2) & kLanes;
+  }
 }
 
-/* Digit-d count among the first t (<= 96) digits of a block (data words
- * q[1..3], 32 digits each). */
-__device__ __forceinline__ uint32_t quad_count(uint64_t const q[4], uint32_t d,
-                                               uint32_t t) {
+/* Digit-d count among the first t digits of a block. */
+template <int W>
+__device__ __forceinline__ uint32_t group_count(uint64_t const q[4], uint32_t d,
+                                                uint32_t t) {
   uint32_t c = 0;
+  if constexpr (W == 2) {
 #pragma unroll
-  for (uint32_t w = 1; w < 4; ++w) {
-    uint32_t const lo = 32 * (w - 1);  // first digit of word w
-    uint64_t const mask = t >= lo + 32 ? ~0ull
-                          : t > lo     ? (1ull << (2 * (t - lo))) - 1
-                                       : 0ull;
-    c += __popcll(quad_match(q[w], d) & mask);
+    for (uint32_t w = 1; w < 4; ++w) {
+      uint32_t const lo = 32 * (w - 1);  // first digit of word w
+      uint64_t const mask = t >= lo + 32 ? ~0ull
+                            : t > lo     ? (1ull << (2 * (t - lo))) - 1
+                                         : 0ull;
+      c += __popcll(group_match<2>(q[w], d) & mask);
+    }
+  } else {
+#pragma unroll
+    for (uint32_t w = 2; w < 4; ++w) {
+      uint32_t const lo = 21 * (w - 2);
+      uint64_t const mask = t >= lo + 21 ? ~0ull
+                            : t > lo     ? (1ull << (3 * (t - lo))) - 1
+                                         : 0ull;
+      c += __popcll(group_match<3>(q[w], d) & mask);
+    }
   }
   return c;
 }
 
-__device__ __forceinline__ uint32_t quad_digit(uint64_t const q[4], uint32_t t) {
-  uint64_t const w = t < 32 ? q[1] : t < 64 ? q[2] : q[3];
-  return static_cast<uint32_t>(w >> (2 * (t & 31))) & 3u;
+template <int W>
+__device__ __forceinline__ uint32_t group_digit(uint64_t const q[4], uint32_t t) {
+  if constexpr (W == 2) {
+    uint64_t const w = t < 32 ? q[1] : t < 64 ? q[2] : q[3];
+    return static_cast<uint32_t>(w >> (2 * (t & 31))) & 3u;
+  } else {
+    uint32_t const hi = t >= 21;
+    uint64_t const w = hi ? q[3] : q[2];
+    return static_cast<uint32_t>(w >> (3 * (t - 21 * hi))) & 7u;
+  }
 }
 
 /* Digit-d count before the block from its header and superblock entry. */
-__device__ __forceinline__ uint64_t quad_before(uint64_t q0, uint64_t sbv,
-                                                uint32_t d, uint64_t blk) {
-  uint32_t const h0 = static_cast<uint32_t>(q0) & 0xFFFFu;
-  uint32_t const h1 = static_cast<uint32_t>(q0 >> 16) & 0xFFFFu;
-  uint32_t const h2 = static_cast<uint32_t>(q0 >> 32) & 0xFFFFu;
-  uint32_t const in_sb = static_cast<uint32_t>(blk % kQuadSbBlocks) * kQuadDigits;
-  uint32_t const h = d == 0 ? h0 : d == 1 ? h1 : d == 2 ? h2 : in_sb - h0 - h1 - h2;
+template <int W>
+__device__ __forceinline__ uint64_t group_before(uint64_t q0, uint64_t q1,
+                                                 uint64_t sbv, uint32_t d,
+                                                 uint64_t blk) {
+  constexpr uint32_t kD = GroupShape<W>::kDigits, kSb = GroupShape<W>::kSbBlocks;
+  uint32_t const in_sb = static_cast<uint32_t>(blk % kSb) * kD;
+  uint32_t h;
+  if constexpr (W == 2) {
+    uint32_t const h0 = static_cast<uint32_t>(q0) & 0xFFFFu;
+    uint32_t const h1 = static_cast<uint32_t>(q0 >> 16) & 0xFFFFu;
+    uint32_t const h2 = static_cast<uint32_t>(q0 >> 32) & 0xFFFFu;
+    h = d == 0 ? h0 : d == 1 ? h1 : d == 2 ? h2 : in_sb - h0 - h1 - h2;
+  } else {
+    uint32_t sum = 0;
+    h = 0;
+#pragma unroll
+    for (uint32_t x = 0; x < 7; ++x) {
+      uint32_t const v = static_cast<uint32_t>((x < 4 ? q0 : q1) >> (16 * (x & 3))) & 0xFFFFu;
+      sum += v;
+      if (x == d) h = v;
+    }
+    if (d == 7) h = in_sb - sum;
+  }
   return sbv + h;
 }
 
-/* Digit at position p < n of quad level ql and its occurrences before p. */
-__device__ __forceinline__ uint32_t quad_access(const QuadView& v,
-                                                QuadLevel const& ql, uint64_t p,
-                                                uint64_t* before) {
-  uint64_t const blk = p / kQuadDigits;
-  uint32_t const t = static_cast<uint32_t>(p - blk * kQuadDigits);
+/* Digit at position p < n of group level ql and its occurrences before p. */
+template <int W>
+__device__ __forceinline__ uint32_t group_access(const QuadView& v,
+                                                 QuadLevel const& ql, uint64_t p,
+                                                 uint64_t* before) {
+  constexpr uint32_t kD = GroupShape<W>::kDigits, kSb = GroupShape<W>::kSbBlocks;
+  uint64_t const blk = p / kD;
+  uint32_t const t = static_cast<uint32_t>(p - blk * kD);
   uint4 const* bp = v.blocks + (ql.blk_off + blk) * 2;
-  uint4 const* sp = reinterpret_cast<uint4 const*>(
-      v.sb + (ql.sb_off + blk / kQuadSbBlocks) * 4);
+  uint64_t const* sp = v.sb + ql.sb_off + (blk / kSb) * (1u << W);
   uint4 const a = __ldg(bp), b = __ldg(bp + 1);
-  uint4 const s0 = __ldg(sp), s1 = __ldg(sp + 1);  // all four digit counts
   uint64_t q[4];
   quad_words(a, b, q);
-  uint32_t const d = quad_digit(q, t);
-  uint64_t const sbv = d == 0 ? ((uint64_t(s0.y) << 32) | s0.x)
-                       : d == 1 ? ((uint64_t(s0.w) << 32) | s0.z)
-                       : d == 2 ? ((uint64_t(s1.y) << 32) | s1.x)
-                                : ((uint64_t(s1.w) << 32) | s1.z);
-  *before = quad_before(q[0], sbv, d, blk) + quad_count(q, d, t);
+  uint32_t const d = group_digit<W>(q, t);
+  uint64_t const sbv = __ldg(sp + d);  // an L2 hit: the table is small
+  *before = group_before<W>(q[0], q[1], sbv, d, blk) + group_count<W>(q, d, t);
   return d;
 }
 
-/* Occurrences of digit d in [0, p) of quad level ql, p <= n. */
-__device__ __forceinline__ uint64_t quad_rank(const QuadView& v,
-                                              QuadLevel const& ql, uint64_t p,
-                                              uint32_t d) {
-  uint64_t const blk = p / kQuadDigits;
-  uint32_t const t = static_cast<uint32_t>(p - blk * kQuadDigits);
+/* Occurrences of digit d in [0, p) of group level ql, p <= n. */
+template <int W>
+__device__ __forceinline__ uint64_t group_rank(const QuadView& v,
+                                               QuadLevel const& ql, uint64_t p,
+                                               uint32_t d) {
+  constexpr uint32_t kD = GroupShape<W>::kDigits, kSb = GroupShape<W>::kSbBlocks;
+  uint64_t const blk = p / kD;
+  uint32_t const t = static_cast<uint32_t>(p - blk * kD);
   uint4 const* bp = v.blocks + (ql.blk_off + blk) * 2;
   uint4 const a = __ldg(bp), b = __ldg(bp + 1);
-  uint64_t const sbv = __ldg(v.sb + (ql.sb_off + blk / kQuadSbBlocks) * 4 + d);
+  uint64_t const sbv = __ldg(v.sb + ql.sb_off + (blk / kSb) * (1u << W) + d);
   uint64_t q[4];
   quad_words(a, b, q);
-  return quad_before(q[0], sbv, d, blk) + quad_count(q, d, t);
+  return group_before<W>(q[0], q[1], sbv, d, blk) + group_count<W>(q, d, t);
 }
 
-/* Position of the k-th (1-based, k <= total[d]) digit d of quad level ql:
- * dense samples bracket its block (without them the superblock table does),
- * a binary search over block counts narrows wide brackets to two blocks,
- * both read at once, then the in-block scan. */
-__device__ __forceinline__ uint64_t quad_select(const QuadView& v,
-                                                QuadLevel const& ql,
-                                                uint32_t d, uint64_t k) {
-  uint64_t const nblk = ql.num_blocks;
-  if (k == 0 || k > ql.total[d]) return nblk * kQuadDigits;  // invalid structure
-  uint64_t const* sb = v.sb + ql.sb_off * 4 + d;
-  uint4 const* blocks = v.blocks + ql.blk_off * 2;
-  uint64_t lo, hi, est;
-  if (v.ds) {
-    uint32_t const sh = v.sel_shift;
-    uint32_t const* S = v.ds + ql.ds_off[d];
-    uint64_t const j = (k - 1) >> sh;
-    lo = min(uint64_t(__ldg(S + j)), nblk - 1);
-    hi = ((j + 1) << sh) < ql.total[d] ? __ldg(S + j + 1) : nblk - 1;
-    hi = min(max(hi, lo), nblk - 1);
-    // the k-th digit sits about (k - 1 - j * R) / R of the way into the
-    // bracket: start there
-    est = lo + (((hi - lo) * ((k - 1) - (j << sh))) >> sh);
-  } else {  // superblock whose count before it is below k
-    uint64_t a = 0, z = (nblk - 1) / kQuadSbBlocks;
-    while (a < z) {
-      uint64_t const mid = (a + z + 1) >> 1;
-      if (__ldg(sb + mid * 4) < k) a = mid; else z = mid - 1;
-    }
-    lo = a * kQuadSbBlocks;
-    hi = min(lo + kQuadSbBlocks - 1, nblk - 1);
-    est = lo;
-  }
-  auto before = [&](uint64_t blk) -> uint64_t {
-    uint4 const h = __ldg(blocks + blk * 2);
-    return quad_before((uint64_t(h.y) << 32) | h.x,
-                       __ldg(sb + (blk / kQuadSbBlocks) * 4), d, blk);
-  };
-  while (hi - lo > 16) {  // wide brackets only (rare digits)
-    uint64_t const mid = (lo + hi + 1) >> 1;
-    if (before(mid) < k) lo = mid; else hi = mid - 1;
-    est = lo;
-  }
-  // from the estimate, one block at a time (query throughput follows the
-  // sectors read): the block holding the k-th digit has fewer than k of them
-  // before it and at least k up to its end
-  uint64_t blk = min(max(est, lo), hi);
-  uint64_t q[4];
-  uint64_t bt = 0;
-  for (uint32_t guard = 0; guard < 24; ++guard) {
-    uint4 const a0 = __ldg(blocks + blk * 2), a1 = __ldg(blocks + blk * 2 + 1);
-    quad_words(a0, a1, q);
-    bt = quad_before(q[0], __ldg(sb + (blk / kQuadSbBlocks) * 4), d, blk);
-    if (bt >= k && blk > lo) {  // it lies before this block
-      hi = blk - 1;
-      --blk;
-      continue;
-    }
-    if (blk < hi && bt + quad_count(q, d, kQuadDigits) < k) {  // after it
-      lo = blk + 1;
-      ++blk;
-      continue;
-    }
-    break;
-  }
-  uint32_t r = static_cast<uint32_t>(k - bt);  // 1 ..= 96
-  uint32_t pos = 0;
+/* Position (in the block) of the r-th digit d, 1 <= r <= its count there;
+ * kD when absent (not reached for valid structures). */
+template <int W>
+__device__ __forceinline__ uint32_t group_select_in(uint64_t const q[4],
+                                                    uint32_t d, uint32_t r) {
+  constexpr uint32_t kFirst = W == 2 ? 1 : 2, kPer = W == 2 ? 32 : 21;
+  uint32_t pos = GroupShape<W>::kDigits;
   bool found = false;
 #pragma unroll
-  for (uint32_t w = 1; w < 4; ++w) {
-    uint64_t const m = quad_match(q[w], d);
+  for (uint32_t w = kFirst; w < 4; ++w) {
+    uint64_t const m = group_match<W>(q[w], d);
     uint32_t const c = __popcll(m);
     if (!found) {
       if (r <= c) {
         uint32_t const lo32 = static_cast<uint32_t>(m);
         uint32_t const cl = __popc(lo32);
-        uint32_t const bit = r <= cl
-                                 ? select_in_word(lo32, r)
-                                 : 32 + select_in_word(static_cast<uint32_t>(m >> 32), r - cl);
-        pos = 32 * (w - 1) + bit / 2;
+        uint32_t const bit =
+            r <= cl ? select_in_word(lo32, r)
+                    : 32 + select_in_word(static_cast<uint32_t>(m >> 32), r - cl);
+        pos = kPer * (w - kFirst) + bit / W;
         found = true;
       } else {
         r -= c;
       }
     }
   }
-  if (!found) return nblk * kQuadDigits;  // not reached for valid structures
-  return blk * kQuadDigits + pos;
+  return pos;
+}
+
+/* Position of the k-th (1-based, k <= total[d]) digit d of group level ql:
+ * dense samples bracket its block (without them the superblock table does),
+ * brackets wider than 16 blocks are narrowed by binary search, then the
+ * search starts at the block the sample rank interpolates to and moves one
+ * block at a time (throughput follows the sectors read). */
+template <int W>
+__device__ __forceinline__ uint64_t group_select(const QuadView& v,
+                                                 QuadLevel const& ql,
+                                                 uint32_t d, uint64_t k) {
+  constexpr uint32_t kD = GroupShape<W>::kDigits, kSb = GroupShape<W>::kSbBlocks;
+  constexpr uint32_t kS = 1u << W;  // superblock-table words per superblock
+  uint64_t const nblk = ql.num_blocks;
+  if (k == 0 || k > ql.total[d]) return nblk * kD;  // invalid structure
+  uint64_t const* sb = v.sb + ql.sb_off + d;
+  uint4 const* blocks = v.blocks + ql.blk_off * 2;
+  uint64_t lo, hi, est;
+  if (v.ds && ql.sel_shift) {
+    uint32_t const sh = ql.sel_shift;
+    uint32_t const* S = v.ds + ql.ds_off[d];
+    uint64_t const j = (k - 1) >> sh;
+    lo = min(uint64_t(__ldg(S + j)), nblk - 1);
+    hi = ((j + 1) << sh) < ql.total[d] ? __ldg(S + j + 1) : nblk - 1;
+    hi = min(max(hi, lo), nblk - 1);
+    est = lo + (((hi - lo) * ((k - 1) - (j << sh))) >> sh);
+  } else {  // superblock whose count before it is below k
+    uint64_t a = 0, z = (nblk - 1) / kSb;
+    while (a < z) {
+      uint64_t const mid = (a + z + 1) >> 1;
+      if (__ldg(sb + mid * kS) < k) a = mid; else z = mid - 1;
+    }
+    lo = a * kSb;
+    hi = min(lo + kSb - 1, nblk - 1);
+    est = lo;
+  }
+  auto before = [&](uint64_t blk) -> uint64_t {
+    uint4 const h = __ldg(blocks + blk * 2);
+    return group_before<W>((uint64_t(h.y) << 32) | h.x, (uint64_t(h.w) << 32) | h.z,
+                           __ldg(sb + (blk / kSb) * kS), d, blk);
+  };
+  while (hi - lo > 16) {  // wide brackets only (rare digits)
+    uint64_t const mid = (lo + hi + 1) >> 1;
+    if (before(mid) < k) lo = mid; else hi = mid - 1;
+    est = lo;
+  }
+  uint64_t blk = min(max(est, lo), hi);
+  uint64_t q[4];
+  uint64_t bt = 0;
+  for (uint32_t guard = 0; guard < 24; ++guard) {
+    uint4 const a0 = __ldg(blocks + blk * 2), a1 = __ldg(blocks + blk * 2 + 1);
+    quad_words(a0, a1, q);
+    bt = group_before<W>(q[0], q[1], __ldg(sb + (blk / kSb) * kS), d, blk);
+    if (bt >= k && blk > lo) {  // it lies before this block
+      hi = blk - 1;
+      --blk;
+      continue;
+    }
+    if (blk < hi && bt + group_count<W>(q, d, kD) < k) {  // after it
+      lo = blk + 1;
+      ++blk;
+      continue;
+    }
+    break;
+  }
+  uint32_t const pos = group_select_in<W>(q, d, static_cast<uint32_t>(k - bt));
+  if (pos >= kD) return nblk * kD;  // not reached for valid structures
+  return blk * kD + pos;
 }
 
 /* ---- tree walks ------------------------------------------------------- */
@@ -598,13 +662,13 @@ __device__ __forceinline__ uint64_t occurrences(const TreeView& t,
   return (c + 1 == t.sigma ? t.n : counts[c + 1]) - counts[c];
 }
 
-/* The three walks over quad levels (power-of-two alphabets): the same
- * descent as the binary walks below, two binary levels per step; an odd
- * last binary level is walked as in the binary code. */
+/* The three walks over group levels (power-of-two alphabets): the same
+ * descent as the binary walks below, w binary levels per step; binary levels
+ * past the groups (at most one) are walked as in the binary code. */
 __device__ __forceinline__ uint64_t quad_node_rank(const TreeView& t,
                                                    QuadLevel const& ql,
                                                    uint64_t g, uint32_t d) {
-  return __ldg(t.quad.node_ranks + ql.nr_off + g * 4 + d);
+  return __ldg(t.quad.node_ranks + ql.nr_off + (g << ql.width) + d);
 }
 
 __device__ __forceinline__ uint64_t wt_access_quad(const TreeView& t,
@@ -615,14 +679,16 @@ __device__ __forceinline__ uint64_t wt_access_quad(const TreeView& t,
   uint64_t cs = 0;
   for (uint32_t j = 0; j < t.quad.num; ++j) {
     QuadLevel const& ql = t.quad.levels[j];
-    uint32_t const sh = L - 2 * j;  // log2 of the symbols under a level-2j node
+    uint32_t const w = ql.width;
+    uint32_t const sh = L - ql.start;  // log2 of the symbols under a node
     uint64_t before;
-    uint32_t const d = quad_access(t.quad, ql, counts[cs] + idx, &before);
-    if (j + 1 < t.quad.num || (L & 1))
+    uint32_t const d = w == 3 ? group_access<3>(t.quad, ql, counts[cs] + idx, &before)
+                              : group_access<2>(t.quad, ql, counts[cs] + idx, &before);
+    if (j + 1 < t.quad.num || t.quad.covered < L)
       idx = before - quad_node_rank(t, ql, cs >> sh, d);
-    cs += uint64_t(d) << (sh - 2);
+    cs += uint64_t(d) << (sh - w);
   }
-  if (L & 1) {  // last binary level: its bit alone
+  if (t.quad.covered < L) {  // last binary level: its bit alone
     if (rs_bit(t.rs, meta[L - 1], counts[cs] + idx)) cs += 1;
   }
   return cs;
@@ -638,13 +704,15 @@ __device__ __forceinline__ uint64_t wt_rank_quad(const TreeView& t,
   uint64_t cs = 0, res = i;
   for (uint32_t j = 0; j < t.quad.num; ++j) {
     QuadLevel const& ql = t.quad.levels[j];
-    uint32_t const sh = L - 2 * j;
-    uint32_t const d = static_cast<uint32_t>(c >> (sh - 2)) & 3u;
-    res = quad_rank(t.quad, ql, counts[cs] + res, d) -
+    uint32_t const w = ql.width;
+    uint32_t const sh = L - ql.start;
+    uint32_t const d = static_cast<uint32_t>(c >> (sh - w)) & ((1u << w) - 1u);
+    uint64_t const p = counts[cs] + res;
+    res = (w == 3 ? group_rank<3>(t.quad, ql, p, d) : group_rank<2>(t.quad, ql, p, d)) -
           quad_node_rank(t, ql, cs >> sh, d);
-    cs += uint64_t(d) << (sh - 2);
+    cs += uint64_t(d) << (sh - w);
   }
-  if (L & 1) {
+  if (t.quad.covered < L) {
     ArrayMeta const& m = meta[L - 1];
     uint64_t const start = cs ? ranks[node_index(t, node_base, cs, L - 1)] : 0;
     uint64_t const p = counts[cs] + res;
@@ -662,7 +730,7 @@ __device__ __forceinline__ uint64_t wt_select_quad(const TreeView& t,
                                                    uint64_t c, uint64_t k) {
   uint32_t const L = t.levels;
   uint64_t res = k;  // 1-based occurrence inside the current node
-  if (L & 1) {
+  if (t.quad.covered < L) {
     ArrayMeta const& m = meta[L - 1];
     uint64_t const cs = c & ~uint64_t(1);
     uint64_t const z = cs ? ranks[node_index(t, node_base, cs, L - 1)] : 0;
@@ -675,11 +743,13 @@ __device__ __forceinline__ uint64_t wt_select_quad(const TreeView& t,
   }
   for (int j = int(t.quad.num) - 1; j >= 0; --j) {
     QuadLevel const& ql = t.quad.levels[j];
-    uint32_t const sh = L - 2 * uint32_t(j);
+    uint32_t const w = ql.width;
+    uint32_t const sh = L - ql.start;
     uint64_t const g = c >> sh;
-    uint32_t const d = static_cast<uint32_t>(c >> (sh - 2)) & 3u;
-    uint64_t const pos =
-        quad_select(t.quad, ql, d, quad_node_rank(t, ql, g, d) + res);
+    uint32_t const d = static_cast<uint32_t>(c >> (sh - w)) & ((1u << w) - 1u);
+    uint64_t const kk = quad_node_rank(t, ql, g, d) + res;
+    uint64_t const pos = w == 3 ? group_select<3>(t.quad, ql, d, kk)
+                                : group_select<2>(t.quad, ql, d, kk);
     res = pos + 1 - counts[g << sh];
   }
   return res - 1;

@@ -41,6 +41,32 @@ def test_u8_boundary_lengths(ewt, oracle, n):
     check_queries(gt, ot, text, al, 2_000, seed=n)
 
 
+# Group query levels: octal superblocks hold 21,504 digits (512 blocks of
+# 42), the routing pass works on 32,768-position superblocks, quad
+# superblocks hold 49,152 digits.  Lengths at those boundaries, for trees of
+# one octal group (sigma 8), octal + quad (32), two octal (64), and octal +
+# two quad (128: 3 + 2 + 2).
+@pytest.mark.parametrize("sigma", [8, 32, 64, 128])
+@pytest.mark.parametrize("n", [41, 42, 43, 21_503, 21_504, 21_505, 32_768 + 1,
+                               2 * 49_152 + 95, 5 * 21_504 + 7 * 42])
+def test_group_level_boundaries(ewt, oracle, sigma, n):
+    rng = np.random.default_rng(sigma * 1_000_003 + n)
+    text = rng.integers(0, sigma, n, dtype=np.uint64).astype(np.uint8)
+    gt, ot, al = build_both(ewt, oracle, text, sigma)
+    check_queries(gt, ot, text, al, 2_000, seed=n)
+
+
+@pytest.mark.parametrize("sigma", [8, 64, 512])
+def test_group_levels_sorted_runs(ewt, oracle, sigma):
+    # every node boundary of every level falls inside some superblock
+    n = 300_000
+    rng = np.random.default_rng(sigma)
+    text = np.sort(rng.integers(0, sigma, n, dtype=np.uint64))
+    text = text.astype(np.uint16 if sigma > 256 else np.uint8)
+    gt, ot, al = build_both(ewt, oracle, text, sigma)
+    check_queries(gt, ot, text, al, 5_000, seed=sigma)
+
+
 @pytest.mark.parametrize("L", [1, 5, 9, 13, 16])
 def test_u16_level_counts(ewt, oracle, L):
     sigma = 1 << L
