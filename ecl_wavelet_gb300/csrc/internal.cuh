@@ -208,7 +208,10 @@ bool quad_eligible(ewt_tree const& t);
 // Digit widths of the group levels of an L-level tree, top down: octal (3)
 // groups, then one or two quad (2) groups; they cover all L levels.
 std::vector<uint32_t> group_widths(uint32_t L);
-void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, cudaStream_t st);
+// sym: the tree's minimal symbols on the device (elem_size bytes each), or
+// null; level 0 is then built from them directly.
+void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
+                uint32_t elem_size, cudaStream_t st);
 void build_quad_samples(ewt_tree& t, uint32_t shift, cudaStream_t st);
 // Dense select samples of the binary and quad levels at rate 2^shift (0:
 // none), and the tree's view updated.

@@ -19,12 +19,14 @@
 //      time through a 64K-entry table in shared memory, block headers from
 //      a scan, blocks and dense select samples written; the superblock's
 //      totals are checked against pass 1.
-// Octal group at l:
+// Octal group at l = 0 of 1- and 2-byte symbols: octal_text_kernel takes the
+// digits straight from the (minimal) symbols.  Other octal groups at l:
 //   1. merge_plane_kernel: level l+2 routed into level-(l+1) order (a plane
 //      of n bits);
 //   2. octal_level_kernel (same shape, one thread per 42-digit block): the
 //      digit's middle and low bits route level l+1 and that plane into
-//      level-l order; headers from a scan; per-superblock counts written;
+//      level-l order; blocks store the three bit planes; headers from a
+//      scan; per-superblock counts written;
 //   3. group_scan_*, then group_samples_kernel (dense samples; the level's
 //      digit totals checked against the count table).
 // Node ranks (digit counts before every node) and digit totals come from
@@ -205,10 +207,13 @@ group_scan_partial_kernel(uint64_t const* __restrict__ sb, uint64_t count,
                           uint64_t* __restrict__ chunk) {
   uint64_t const first = uint64_t(blockIdx.x) * kScanChunk;
   uint64_t c[S];
+#pragma unroll
   for (uint32_t d = 0; d < S; ++d) c[d] = 0;
   for (uint64_t i = first + threadIdx.x; i < min(count, first + kScanChunk);
        i += blockDim.x)
+#pragma unroll
     for (uint32_t d = 0; d < S; ++d) c[d] += sb[i * S + d];
+#pragma unroll
   for (uint32_t d = 0; d < S; ++d) {
     uint64_t tot = 0;
     cta_exclusive_scan(c[d], &tot);
@@ -279,7 +284,8 @@ void scan_superblocks(uint64_t* sb, uint64_t entries, DevBuf& chunk, cudaStream_
 
 // Dense samples of one block: entry k of digit d names the block holding
 // its (k * 2^sel_shift + 1)-th occurrence; before/c = occurrences before /
-// in it (S = 2^width digits).
+// in it (S = 2^width digits).  Entry k lies in the block iff
+// before <= k * R < before + c.
 template <uint32_t S>
 __device__ __forceinline__ void put_group_samples(uint32_t* __restrict__ ds,
                                                   QuadLevel const& ql, uint64_t blk,
@@ -289,14 +295,11 @@ __device__ __forceinline__ void put_group_samples(uint32_t* __restrict__ ds,
   uint64_t const R = uint64_t(1) << sh;
 #pragma unroll
   for (uint32_t d = 0; d < S; ++d) {
-    if (c[d] == 0) continue;
-    // entries fit in 32 bits (at most n / 16 of them)
-    uint32_t const entries = static_cast<uint32_t>((ql.total[d] + R - 1) >> sh);
-    uint32_t const last =
-        min(static_cast<uint32_t>((before[d] + c[d] - 1) >> sh), entries - 1);
+    uint64_t const end = before[d] + c[d];
+    uint64_t k = (before[d] + R - 1) >> sh;
+    if ((k << sh) >= end) continue;  // the common case: no entry here
     uint32_t* S_ = ds + ql.ds_off[d];
-    for (uint32_t k = static_cast<uint32_t>((before[d] + R - 1) >> sh); k <= last; ++k)
-      S_[k] = static_cast<uint32_t>(blk);
+    for (; (k << sh) < end; ++k) S_[k] = static_cast<uint32_t>(blk);
   }
 }
 
@@ -641,17 +644,6 @@ merge_plane_kernel(TreeView v, uint32_t l, uint32_t const* __restrict__ hi_w,
   }
 }
 
-// Bits k of x (k < 21) to bits 3k.
-__device__ __forceinline__ uint64_t spread3(uint64_t x) {
-  x &= 0x1FFFFFull;
-  x = (x | (x << 32)) & 0x1F00000000FFFFull;
-  x = (x | (x << 16)) & 0x1F0000FF0000FFull;
-  x = (x | (x << 8)) & 0x100F00F00F00F00Full;
-  x = (x | (x << 4)) & 0x10C30C30C30C30C3ull;
-  x = (x | (x << 2)) & 0x1249249249249249ull;
-  return x;
-}
-
 // Exclusive scan of four uint32 over one 512-thread half (as
 // group_exclusive_scan32, one set of barriers).
 __device__ __forceinline__ uint4 group_exclusive_scan4(uint4 x, uint4* total) {
@@ -759,10 +751,124 @@ octal_level_kernel(TreeView v, uint32_t l, uint32_t const* __restrict__ hi_w,
       for (uint32_t d = 0; d < 8; ++d) o[d] = (w4[d >> 1] >> (16 * (d & 1))) & 0xFFFFu;
     }
     if (!mine) continue;
-    uint64_t const w2 = (spread3(H) << 2) | (spread3(M) << 1) | spread3(B);
-    uint64_t const w3 = (spread3(H >> 21) << 2) | (spread3(M >> 21) << 1) | spread3(B >> 21);
+    // planes H, M, B in words 1..3, counts of digits 4..6 above them
+    uint64_t const w1 = H | (uint64_t(e.z & 0xFFFFu) << 42);
+    uint64_t const w2 = M | (uint64_t(e.z >> 16) << 42);
+    uint64_t const w3 = B | (uint64_t(e.w & 0xFFFFu) << 42);
     uint4* out = blocks + blk * 2;
-    out[0] = make_uint4(e.x, e.y, e.z, e.w & 0xFFFFu);
+    out[0] = make_uint4(e.x, e.y, static_cast<uint32_t>(w1), static_cast<uint32_t>(w1 >> 32));
+    out[1] = make_uint4(static_cast<uint32_t>(w2), static_cast<uint32_t>(w2 >> 32),
+                        static_cast<uint32_t>(w3), static_cast<uint32_t>(w3 >> 32));
+  }
+}
+
+// Octal level 0 of a tree of 1- or 2-byte minimal symbols, straight from
+// the symbols (digit = their top three bits; no routing): persistent CTAs of
+// 1024 threads, each 512-thread half on its own superblocks.  The half
+// first turns the superblock's symbols (16-byte loads) into three bit planes
+// in shared memory, then each thread takes its block's 42 bits of each.
+template <class T>
+__global__ void __launch_bounds__(1024, 1)
+octal_text_kernel(T const* __restrict__ sym, uint64_t n, uint32_t L, uint64_t nsb,
+                  uint64_t num_blocks, uint4* __restrict__ blocks,
+                  uint64_t* __restrict__ sb) {
+  constexpr uint32_t kV = 16 / sizeof(T);           // symbols per 16-byte load
+  constexpr uint32_t kLoads = uint32_t(kOctSbDigits) / kV;
+  constexpr uint32_t kWords = uint32_t(kOctSbDigits) / 32 + 4;
+  __shared__ uint32_t planes[2][3][kWords];
+  uint32_t const half = threadIdx.x >> 9;
+  uint32_t const t = threadIdx.x & (kOctSbBlocks - 1);
+  uint32_t const sb0 = L - 3;  // bit of the digit's lowest plane
+  constexpr uint32_t kPer = (kLoads + kOctSbBlocks - 1) / kOctSbBlocks;  // loads / thread
+  uint64_t const first = uint64_t(blockIdx.x) * 2 + half;
+  uint64_t const stride = uint64_t(gridDim.x) * 2;
+  // The next superblock's symbols are loaded while this one is processed.
+  auto load = [&](uint64_t sbi, uint4 (&x)[kPer]) {
+    uint64_t const base = sbi * kOctSbDigits;
+#pragma unroll
+    for (uint32_t j = 0; j < kPer; ++j) {
+      uint32_t const u = t + j * kOctSbBlocks;
+      uint64_t const pos = base + uint64_t(u) * kV;
+      x[j] = make_uint4(0, 0, 0, 0);
+      if (sbi >= nsb || u >= kLoads) continue;
+      if (pos + kV <= n) {
+        x[j] = __ldg(reinterpret_cast<uint4 const*>(sym + pos));
+      } else if (pos < n) {
+        T e[kV];
+        for (uint32_t i = 0; i < kV; ++i) e[i] = pos + i < n ? sym[pos + i] : T(0);
+        x[j] = *reinterpret_cast<uint4 const*>(e);
+      }
+    }
+  };
+  uint4 nx[kPer];
+  load(first, nx);
+  for (uint64_t sbi = first; sbi < nsb; sbi += stride) {
+    uint4 cx[kPer];
+#pragma unroll
+    for (uint32_t j = 0; j < kPer; ++j) cx[j] = nx[j];
+    load(sbi + stride, nx);
+#pragma unroll
+    for (uint32_t j = 0; j < kPer; ++j) {
+      uint32_t const u = t + j * kOctSbBlocks;
+      if (u >= kLoads) continue;
+      uint32_t const w[4] = {cx[j].x, cx[j].y, cx[j].z, cx[j].w};
+#pragma unroll
+      for (uint32_t b = 0; b < 3; ++b) {  // plane b: bit sb0 + 2 - b
+        uint32_t const sh = sb0 + 2 - b;
+        uint32_t f = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < 4; ++k) {
+          if constexpr (sizeof(T) == 1) {
+            uint32_t const m = (w[k] >> sh) & 0x01010101u;
+            f |= (((m * 0x00204081u) >> 21) & 0xFu) << (4 * k);
+          } else {
+            uint32_t const m = (w[k] >> sh) & 0x00010001u;
+            f |= ((m | (m >> 15)) & 3u) << (2 * k);
+          }
+        }
+        if constexpr (sizeof(T) == 1)
+          reinterpret_cast<uint16_t*>(planes[half][b])[u] = static_cast<uint16_t>(f);
+        else
+          reinterpret_cast<uint8_t*>(planes[half][b])[u] = static_cast<uint8_t>(f);
+      }
+    }
+    asm volatile("bar.sync %0, 512;" ::"r"(half + 1) : "memory");
+    uint64_t const blk = sbi * kOctSbBlocks + t;
+    bool const mine = blk < num_blocks;
+    uint64_t const p = blk * kOctDigits;
+    uint32_t const valid =
+        mine && p < n ? static_cast<uint32_t>(min(uint64_t(kOctDigits), n - p)) : 0u;
+    uint64_t const vm = (1ull << valid) - 1;
+    uint32_t const o = t * kOctDigits, wi = o >> 5, s = o & 31;
+    uint64_t pl[3];
+#pragma unroll
+    for (uint32_t b = 0; b < 3; ++b) {
+      uint32_t const* P = planes[half][b];
+      pl[b] = (uint64_t(__funnelshift_r(P[wi], P[wi + 1], s)) |
+               (uint64_t(__funnelshift_r(P[wi + 1], P[wi + 2], s)) << 32)) & vm;
+    }
+    uint64_t const H = pl[0], M = pl[1], B = pl[2];
+    uint32_t c[8];
+#pragma unroll
+    for (uint32_t d = 0; d < 8; ++d)
+      c[d] = __popcll((d & 4 ? H : ~H) & (d & 2 ? M : ~M) & (d & 1 ? B : ~B) & vm);
+    uint4 tot4;
+    uint4 const e = group_exclusive_scan4(
+        make_uint4(c[0] | (c[1] << 16), c[2] | (c[3] << 16), c[4] | (c[5] << 16),
+                   c[6] | (c[7] << 16)),
+        &tot4);  // its barriers also end this superblock's plane reads
+    if (t == 0) {
+      uint64_t* out = sb + sbi * 8;
+      uint32_t const w4[4] = {tot4.x, tot4.y, tot4.z, tot4.w};
+#pragma unroll
+      for (uint32_t d = 0; d < 8; ++d) out[d] = (w4[d >> 1] >> (16 * (d & 1))) & 0xFFFFu;
+    }
+    if (!mine) continue;
+    uint64_t const w1 = H | (uint64_t(e.z & 0xFFFFu) << 42);
+    uint64_t const w2 = M | (uint64_t(e.z >> 16) << 42);
+    uint64_t const w3 = B | (uint64_t(e.w & 0xFFFFu) << 42);
+    uint4* out = blocks + blk * 2;
+    out[0] = make_uint4(e.x, e.y, static_cast<uint32_t>(w1), static_cast<uint32_t>(w1 >> 32));
     out[1] = make_uint4(static_cast<uint32_t>(w2), static_cast<uint32_t>(w2 >> 32),
                         static_cast<uint32_t>(w3), static_cast<uint32_t>(w3 >> 32));
   }
@@ -792,20 +898,41 @@ group_samples_kernel(uint4 const* __restrict__ blocks, uint64_t const* __restric
   uint64_t const* sbv = sb + (b / kSb) * S;
   uint64_t before[S];
   uint32_t c[S];
+  if constexpr (W == 3) {  // headers parsed once, counts from the planes
+    uint64_t const vm = (1ull << valid) - 1;
+    uint64_t const H = q[1] & vm, M = q[2] & vm, B = q[3] & vm;
+    uint32_t h[8];
+    h[0] = static_cast<uint32_t>(q[0]) & 0xFFFFu;
+    h[1] = static_cast<uint32_t>(q[0] >> 16) & 0xFFFFu;
+    h[2] = static_cast<uint32_t>(q[0] >> 32) & 0xFFFFu;
+    h[3] = static_cast<uint32_t>(q[0] >> 48);
+    h[4] = static_cast<uint32_t>(q[1] >> 42) & 0xFFFFu;
+    h[5] = static_cast<uint32_t>(q[2] >> 42) & 0xFFFFu;
+    h[6] = static_cast<uint32_t>(q[3] >> 42) & 0xFFFFu;
+    h[7] = static_cast<uint32_t>(b % kSb) * kD - h[0] - h[1] - h[2] - h[3] - h[4] -
+           h[5] - h[6];
 #pragma unroll
-  for (uint32_t d = 0; d < S; ++d) {
-    c[d] = ecl::detail::group_count<W>(q, d, valid);
-    before[d] = ecl::detail::group_before<W>(q[0], q[1], sbv[d], d, b);
+    for (uint32_t d = 0; d < S; ++d) {
+      c[d] = __popcll((d & 4 ? H : ~H) & (d & 2 ? M : ~M) & (d & 1 ? B : ~B) & vm);
+      before[d] = sbv[d] + h[d];
+    }
+  } else {
+#pragma unroll
+    for (uint32_t d = 0; d < S; ++d) {
+      c[d] = ecl::detail::group_count<W>(q, d, valid);
+      before[d] = ecl::detail::group_before<W>(q, sbv[d], d, b);
+    }
   }
   put_group_samples<S>(ds, ql, b, before, c);
 }
 
 // Sample shift of a group level for the tree-wide rate 2^shift: octal
-// digits are about half as frequent and blocks hold 42 instead of 96, so
-// octal levels sample 4 times as densely (same blocks per bracket).
+// digits are about half as frequent and blocks hold 42 instead of 96, and
+// the interpolated block is off by more blocks at equal bracket width, so
+// octal levels sample 8 times as densely.
 uint32_t level_shift(uint32_t width, uint32_t shift) {
   if (shift == 0) return 0;
-  return width == 3 ? std::max<uint32_t>(shift, 6) - 2 : shift;
+  return width == 3 ? std::max<uint32_t>(shift, 7) - 3 : shift;
 }
 
 // Lays out the dense samples of every group level at rate 2^shift.
@@ -876,7 +1003,8 @@ QuadView QuadStore::view() const {
 
 bool quad_eligible(ewt_tree const& t) { return t.pow2 && t.L >= 2 && t.n >= 1; }
 
-void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, cudaStream_t st) {
+void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
+                uint32_t elem_size, cudaStream_t st) {
   QuadStore& qs = t.quad;
   qs.levels.clear();
   qs.blocks.reset();
@@ -988,6 +1116,21 @@ void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, cudaStream_t st) {
       EWT_LAUNCHED();
       continue;
     }
+    uint64_t const nsb = ceil_div(ql.num_blocks, uint64_t(kOctSbBlocks));
+    uint32_t const grid_o =
+        static_cast<uint32_t>(std::min<uint64_t>(ceil_div(nsb, 2), uint64_t(sms)));
+    if (lv == 0 && sym && elem_size <= 2) {  // straight from the symbols
+      EWT_CUDA(cudaMemsetAsync(sb + nsb * 8, 0, 64, st));  // the totals entry
+      if (elem_size == 1)
+        octal_text_kernel<uint8_t><<<grid_o, 1024, 0, st>>>(
+            static_cast<uint8_t const*>(sym), n, L, nsb, ql.num_blocks, blocks, sb);
+      else
+        octal_text_kernel<uint16_t><<<grid_o, 1024, 0, st>>>(
+            static_cast<uint16_t const*>(sym), n, L, nsb, ql.num_blocks, blocks, sb);
+      EWT_LAUNCHED();
+      scan_superblocks<8>(sb, nsb + 1, chunk, st);
+      continue;
+    }
     // octal: level lv+2 routed into level-(lv+1) order first
     ArrayMeta const& m2 = t.rs.meta[lv + 2];
     uint64_t const nsb_m = ceil_div(n, kMergeSbPos);
@@ -1001,14 +1144,11 @@ void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, cudaStream_t st) {
         lut8_d.as<uint8_t>(), info.as<SbStart>(), nsb_m, plane.as<uint32_t>(),
         err_d.as<uint32_t>());
     EWT_LAUNCHED();
-    uint64_t const nsb = ceil_div(ql.num_blocks, uint64_t(kOctSbBlocks));
     sb_info_kernel<<<static_cast<uint32_t>(ceil_div(nsb, 128)), 128, 0, st>>>(
         v, lv, kOctSbDigits, nsb, info.as<SbStart>());
     EWT_LAUNCHED();
     EWT_CUDA(cudaMemsetAsync(sb + nsb * 8, 0, 64, st));  // the totals entry
-    octal_level_kernel<<<static_cast<uint32_t>(
-                             std::min<uint64_t>(ceil_div(nsb, 2), uint64_t(sms))),
-                         1024, 65536, st>>>(
+    octal_level_kernel<<<grid_o, 1024, 65536, st>>>(
         v, lv, words + m0.word_off, words + m1.word_off, total_words - m1.word_off,
         plane.as<uint32_t>(), plane_words, lut8_d.as<uint8_t>(), info.as<SbStart>(), nsb,
         ql.num_blocks, blocks, sb, err_d.as<uint32_t>());

@@ -873,7 +873,7 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   t.counts.assign(c.begin(), c.begin() + sigma);
   t.occ.resize(sigma);
   for (uint64_t i = 0; i < sigma; ++i) t.occ[i] = c[i + 1] - c[i];
-  build_quad(t, c, st);
+  build_quad(t, c, sym, sizeof(T), st);
   v.quad = t.quad.view();
 }
 

@@ -98,9 +98,10 @@ struct RSView {
  * counts before every superblock (uint64).
  *   w = 2 (quad): bits 0..47 counts, bits 64..255 96 digits (digit t at bit
  *         64 + 2t), 512 blocks per superblock (49,152 digits);
- *   w = 3 (octal): bits 0..111 counts, two 64-bit words of 21 digits each
- *         (digit t at bit 3 (t mod 21) of word 2 + t / 21), 512 blocks per
- *         superblock (21,504 digits).
+ *   w = 3 (octal): three 42-bit planes (bit 2, 1, 0 of each digit; digit t
+ *         at bit t) in the low bits of words 1..3, counts of digits 0..3 in
+ *         word 0 and of digits 4..6 in bits 42..57 of words 1..3; 512 blocks
+ *         per superblock (21,504 digits).
  * Dense select samples per digit name the block holding every R-th
  * occurrence (uint32); node_ranks[group][node][digit] = occurrences of the
  * digit before the node. */
@@ -417,44 +418,38 @@ __device__ __forceinline__ void quad_words(uint4 a, uint4 b, uint64_t q[4]) {
   q[3] = (uint64_t(b.w) << 32) | b.z;
 }
 
-/* Lane-match masks: the lowest bit of every W-bit lane of q equal to d. */
-template <int W>
-__device__ __forceinline__ uint64_t group_match(uint64_t q, uint32_t d) {
-  if constexpr (W == 2) {
-    uint64_t const e = ~(q ^ (0x5555555555555555ull * d));
-    return e & (e >> 1) & 0x5555555555555555ull;
-  } else {
-    constexpr uint64_t kLanes = 0x1249249249249249ull & ((1ull << 63) - 1);  // 21 lanes
-    uint64_t const e = ~(q ^ (kLanes * d));
-    return e & (e >> 1) & (e >> 2) & kLanes;
-  }
+/* Quad lane-match mask: the lower bit of every 2-bit lane of q equal to d. */
+__device__ __forceinline__ uint64_t quad_match(uint64_t q, uint32_t d) {
+  uint64_t const e = ~(q ^ (0x5555555555555555ull * d));
+  return e & (e >> 1) & 0x5555555555555555ull;
+}
+
+constexpr uint64_t kOctPlane = (1ull << 42) - 1;
+
+/* Octal: bit t set where digit t of the block equals d. */
+__device__ __forceinline__ uint64_t oct_match(uint64_t const q[4], uint32_t d) {
+  return (d & 4 ? q[1] : ~q[1]) & (d & 2 ? q[2] : ~q[2]) & (d & 1 ? q[3] : ~q[3]) &
+         kOctPlane;
 }
 
 /* Digit-d count among the first t digits of a block. */
 template <int W>
 __device__ __forceinline__ uint32_t group_count(uint64_t const q[4], uint32_t d,
                                                 uint32_t t) {
-  uint32_t c = 0;
   if constexpr (W == 2) {
+    uint32_t c = 0;
 #pragma unroll
     for (uint32_t w = 1; w < 4; ++w) {
       uint32_t const lo = 32 * (w - 1);  // first digit of word w
       uint64_t const mask = t >= lo + 32 ? ~0ull
                             : t > lo     ? (1ull << (2 * (t - lo))) - 1
                                          : 0ull;
-      c += __popcll(group_match<2>(q[w], d) & mask);
+      c += __popcll(quad_match(q[w], d) & mask);
     }
+    return c;
   } else {
-#pragma unroll
-    for (uint32_t w = 2; w < 4; ++w) {
-      uint32_t const lo = 21 * (w - 2);
-      uint64_t const mask = t >= lo + 21 ? ~0ull
-                            : t > lo     ? (1ull << (3 * (t - lo))) - 1
-                                         : 0ull;
-      c += __popcll(group_match<3>(q[w], d) & mask);
-    }
+    return __popcll(oct_match(q, d) & ((1ull << t) - 1));  // t <= 42
   }
-  return c;
 }
 
 template <int W>
@@ -463,37 +458,49 @@ __device__ __forceinline__ uint32_t group_digit(uint64_t const q[4], uint32_t t)
     uint64_t const w = t < 32 ? q[1] : t < 64 ? q[2] : q[3];
     return static_cast<uint32_t>(w >> (2 * (t & 31))) & 3u;
   } else {
-    uint32_t const hi = t >= 21;
-    uint64_t const w = hi ? q[3] : q[2];
-    return static_cast<uint32_t>(w >> (3 * (t - 21 * hi))) & 7u;
+    return (static_cast<uint32_t>(q[1] >> t) & 1u) << 2 |
+           (static_cast<uint32_t>(q[2] >> t) & 1u) << 1 |
+           (static_cast<uint32_t>(q[3] >> t) & 1u);
   }
 }
 
 /* Digit-d count before the block from its header and superblock entry. */
 template <int W>
-__device__ __forceinline__ uint64_t group_before(uint64_t q0, uint64_t q1,
-                                                 uint64_t sbv, uint32_t d,
-                                                 uint64_t blk) {
+__device__ __forceinline__ uint64_t group_before(uint64_t const q[4], uint64_t sbv,
+                                                 uint32_t d, uint64_t blk) {
   constexpr uint32_t kD = GroupShape<W>::kDigits, kSb = GroupShape<W>::kSbBlocks;
   uint32_t const in_sb = static_cast<uint32_t>(blk % kSb) * kD;
+  uint64_t const q0 = q[0];
+  uint32_t const h0 = static_cast<uint32_t>(q0) & 0xFFFFu;
+  uint32_t const h1 = static_cast<uint32_t>(q0 >> 16) & 0xFFFFu;
+  uint32_t const h2 = static_cast<uint32_t>(q0 >> 32) & 0xFFFFu;
   uint32_t h;
   if constexpr (W == 2) {
-    uint32_t const h0 = static_cast<uint32_t>(q0) & 0xFFFFu;
-    uint32_t const h1 = static_cast<uint32_t>(q0 >> 16) & 0xFFFFu;
-    uint32_t const h2 = static_cast<uint32_t>(q0 >> 32) & 0xFFFFu;
     h = d == 0 ? h0 : d == 1 ? h1 : d == 2 ? h2 : in_sb - h0 - h1 - h2;
   } else {
-    uint32_t sum = 0;
-    h = 0;
-#pragma unroll
-    for (uint32_t x = 0; x < 7; ++x) {
-      uint32_t const v = static_cast<uint32_t>((x < 4 ? q0 : q1) >> (16 * (x & 3))) & 0xFFFFu;
-      sum += v;
-      if (x == d) h = v;
-    }
-    if (d == 7) h = in_sb - sum;
+    uint32_t const h3 = static_cast<uint32_t>(q0 >> 48);
+    uint32_t const h4 = static_cast<uint32_t>(q[1] >> 42) & 0xFFFFu;
+    uint32_t const h5 = static_cast<uint32_t>(q[2] >> 42) & 0xFFFFu;
+    uint32_t const h6 = static_cast<uint32_t>(q[3] >> 42) & 0xFFFFu;
+    uint32_t const lo = d & 2 ? (d & 1 ? h3 : h2) : (d & 1 ? h1 : h0);
+    uint32_t const hi = d & 2 ? (d & 1 ? in_sb - h0 - h1 - h2 - h3 - h4 - h5 - h6 : h6)
+                              : (d & 1 ? h5 : h4);
+    h = d & 4 ? hi : lo;
   }
   return sbv + h;
+}
+
+/* Superblock entry of digit d from the entries loaded ahead of the block
+ * (so that the table read does not wait for the digit). */
+template <int W>
+__device__ __forceinline__ uint64_t sb_pick(uint4 const e[1u << (W - 1)], uint32_t d) {
+  uint4 u;
+  if constexpr (W == 2) {
+    u = d & 2 ? e[1] : e[0];
+  } else {
+    u = d & 4 ? (d & 2 ? e[3] : e[2]) : (d & 2 ? e[1] : e[0]);
+  }
+  return d & 1 ? (uint64_t(u.w) << 32 | u.z) : (uint64_t(u.y) << 32 | u.x);
 }
 
 /* Digit at position p < n of group level ql and its occurrences before p. */
@@ -502,16 +509,20 @@ __device__ __forceinline__ uint32_t group_access(const QuadView& v,
                                                  QuadLevel const& ql, uint64_t p,
                                                  uint64_t* before) {
   constexpr uint32_t kD = GroupShape<W>::kDigits, kSb = GroupShape<W>::kSbBlocks;
+  constexpr uint32_t kE = 1u << (W - 1);  // uint4 per superblock entry
   uint64_t const blk = p / kD;
   uint32_t const t = static_cast<uint32_t>(p - blk * kD);
   uint4 const* bp = v.blocks + (ql.blk_off + blk) * 2;
-  uint64_t const* sp = v.sb + ql.sb_off + (blk / kSb) * (1u << W);
+  uint4 const* sp =
+      reinterpret_cast<uint4 const*>(v.sb + ql.sb_off + (blk / kSb) * (1u << W));
+  uint4 e[kE];
+#pragma unroll
+  for (uint32_t k = 0; k < kE; ++k) e[k] = __ldg(sp + k);  // L2 hits, in parallel
   uint4 const a = __ldg(bp), b = __ldg(bp + 1);
   uint64_t q[4];
   quad_words(a, b, q);
   uint32_t const d = group_digit<W>(q, t);
-  uint64_t const sbv = __ldg(sp + d);  // an L2 hit: the table is small
-  *before = group_before<W>(q[0], q[1], sbv, d, blk) + group_count<W>(q, d, t);
+  *before = group_before<W>(q, sb_pick<W>(e, d), d, blk) + group_count<W>(q, d, t);
   return d;
 }
 
@@ -528,7 +539,7 @@ __device__ __forceinline__ uint64_t group_rank(const QuadView& v,
   uint64_t const sbv = __ldg(v.sb + ql.sb_off + (blk / kSb) * (1u << W) + d);
   uint64_t q[4];
   quad_words(a, b, q);
-  return group_before<W>(q[0], q[1], sbv, d, blk) + group_count<W>(q, d, t);
+  return group_before<W>(q, sbv, d, blk) + group_count<W>(q, d, t);
 }
 
 /* Position (in the block) of the r-th digit d, 1 <= r <= its count there;
@@ -536,28 +547,36 @@ __device__ __forceinline__ uint64_t group_rank(const QuadView& v,
 template <int W>
 __device__ __forceinline__ uint32_t group_select_in(uint64_t const q[4],
                                                     uint32_t d, uint32_t r) {
-  constexpr uint32_t kFirst = W == 2 ? 1 : 2, kPer = W == 2 ? 32 : 21;
-  uint32_t pos = GroupShape<W>::kDigits;
-  bool found = false;
+  if constexpr (W == 2) {
+    uint32_t pos = GroupShape<W>::kDigits;
+    bool found = false;
 #pragma unroll
-  for (uint32_t w = kFirst; w < 4; ++w) {
-    uint64_t const m = group_match<W>(q[w], d);
-    uint32_t const c = __popcll(m);
-    if (!found) {
-      if (r <= c) {
-        uint32_t const lo32 = static_cast<uint32_t>(m);
-        uint32_t const cl = __popc(lo32);
-        uint32_t const bit =
-            r <= cl ? select_in_word(lo32, r)
-                    : 32 + select_in_word(static_cast<uint32_t>(m >> 32), r - cl);
-        pos = kPer * (w - kFirst) + bit / W;
-        found = true;
-      } else {
-        r -= c;
+    for (uint32_t w = 1; w < 4; ++w) {
+      uint64_t const m = quad_match(q[w], d);
+      uint32_t const c = __popcll(m);
+      if (!found) {
+        if (r <= c) {
+          uint32_t const lo32 = static_cast<uint32_t>(m);
+          uint32_t const cl = __popc(lo32);
+          uint32_t const bit =
+              r <= cl ? select_in_word(lo32, r)
+                      : 32 + select_in_word(static_cast<uint32_t>(m >> 32), r - cl);
+          pos = 32 * (w - 1) + bit / 2;
+          found = true;
+        } else {
+          r -= c;
+        }
       }
     }
+    return pos;
+  } else {
+    uint64_t const m = oct_match(q, d);
+    if (r > static_cast<uint32_t>(__popcll(m))) return GroupShape<W>::kDigits;
+    uint32_t const lo32 = static_cast<uint32_t>(m);
+    uint32_t const cl = __popc(lo32);
+    return r <= cl ? select_in_word(lo32, r)
+                   : 32 + select_in_word(static_cast<uint32_t>(m >> 32), r - cl);
   }
-  return pos;
 }
 
 /* Position of the k-th (1-based, k <= total[d]) digit d of group level ql:
@@ -595,9 +614,9 @@ __device__ __forceinline__ uint64_t group_select(const QuadView& v,
     est = lo;
   }
   auto before = [&](uint64_t blk) -> uint64_t {
-    uint4 const h = __ldg(blocks + blk * 2);
-    return group_before<W>((uint64_t(h.y) << 32) | h.x, (uint64_t(h.w) << 32) | h.z,
-                           __ldg(sb + (blk / kSb) * kS), d, blk);
+    uint64_t h[4];
+    quad_words(__ldg(blocks + blk * 2), __ldg(blocks + blk * 2 + 1), h);
+    return group_before<W>(h, __ldg(sb + (blk / kSb) * kS), d, blk);
   };
   while (hi - lo > 16) {  // wide brackets only (rare digits)
     uint64_t const mid = (lo + hi + 1) >> 1;
@@ -610,7 +629,7 @@ __device__ __forceinline__ uint64_t group_select(const QuadView& v,
   for (uint32_t guard = 0; guard < 24; ++guard) {
     uint4 const a0 = __ldg(blocks + blk * 2), a1 = __ldg(blocks + blk * 2 + 1);
     quad_words(a0, a1, q);
-    bt = group_before<W>(q[0], q[1], __ldg(sb + (blk / kSb) * kS), d, blk);
+    bt = group_before<W>(q, __ldg(sb + (blk / kSb) * kS), d, blk);
     if (bt >= k && blk > lo) {  // it lies before this block
       hi = blk - 1;
       --blk;
