@@ -42,6 +42,16 @@ GIB = 1 << 30
 KINDS = ("access", "rank", "select", "mixed")
 
 
+
+def group_levels(L):
+    """Query levels of a power-of-two tree with L binary levels: octal (3-bit)
+    groups, then one or two quad (2-bit) groups, covering all L levels (the
+    library's plan); a one-level tree is walked binary."""
+    if L < 2:
+        return L
+    quads = 0 if L % 3 == 0 else (1 if L % 3 == 2 else 2)
+    return (L - 2 * quads) // 3 + quads
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -761,7 +771,7 @@ def run_ours(args, world, rank, local):
     # random-access roofline: dependent random 32-byte reads per second
     probe = E.probe_random_reads(8 * GIB, 4, 1 << 25, local)
     L_ = int(tree.info.levels)
-    steps = L_ // 2 + (L_ & 1)  # quad levels (+ an odd binary level)
+    steps = group_levels(L_)
     reads = {"access": steps, "rank": steps, "select": 2 * steps}
     reads["mixed"] = 0.4 * reads["access"] + 0.4 * reads["rank"] + 0.2 * reads["select"]
     rates = {"access": acc_idx.numel() / acc_ms / 1e3 * 1e6,
@@ -769,9 +779,9 @@ def run_ours(args, world, rank, local):
              "select": sq.shape[0] / sel_ms / 1e3 * 1e6,
              "mixed": m / mixed_ms / 1e3 * 1e6}
     rroof = {"probe_reads_per_s": probe,
-             "model": "block reads per query: one per quad level for access and "
-                      "rank, a sample and a block per level for select (a lower "
-                      "bound: wide brackets read more)",
+             "model": "block reads per query: one per group level (octal or "
+                      "quad) for access and rank, a sample and a block per level "
+                      "for select (a lower bound: wide brackets read more)",
              "reads_per_query": reads,
              "frac": {k: rates[k] * reads[k] / probe for k in reads}}
     queries = {

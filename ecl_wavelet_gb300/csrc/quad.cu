@@ -283,23 +283,24 @@ void scan_superblocks(uint64_t* sb, uint64_t entries, DevBuf& chunk, cudaStream_
 }
 
 // Dense samples of one block: entry k of digit d names the block holding
-// its (k * 2^sel_shift + 1)-th occurrence; before/c = occurrences before /
-// in it (S = 2^width digits).  Entry k lies in the block iff
-// before <= k * R < before + c.
+// its (k * R + 1)-th occurrence, R = 2^sel_shift <= 2^16; before/c =
+// occurrences before / in it (S = 2^width digits).  The first multiple of R
+// at or after `before` is before + ((R - before) mod R): an entry lies in the
+// block iff that offset is below c (32-bit test; 64-bit work only then).
 template <uint32_t S>
 __device__ __forceinline__ void put_group_samples(uint32_t* __restrict__ ds,
                                                   QuadLevel const& ql, uint64_t blk,
                                                   uint64_t const before[S],
                                                   uint32_t const c[S]) {
   uint32_t const sh = ql.sel_shift;
-  uint64_t const R = uint64_t(1) << sh;
+  uint32_t const rm = (1u << sh) - 1u;
 #pragma unroll
   for (uint32_t d = 0; d < S; ++d) {
-    uint64_t const end = before[d] + c[d];
-    uint64_t k = (before[d] + R - 1) >> sh;
-    if ((k << sh) >= end) continue;  // the common case: no entry here
+    uint32_t const off = (0u - static_cast<uint32_t>(before[d])) & rm;
+    if (off >= c[d]) continue;  // the common case: no entry here
     uint32_t* S_ = ds + ql.ds_off[d];
-    for (; (k << sh) < end; ++k) S_[k] = static_cast<uint32_t>(blk);
+    uint64_t k = (before[d] + off) >> sh;
+    for (uint32_t o = off; o < c[d]; o += rm + 1, ++k) S_[k] = static_cast<uint32_t>(blk);
   }
 }
 
@@ -524,6 +525,40 @@ __device__ __forceinline__ uint64_t route_runs(uint8_t const* lut, uint64_t h,
   return out;
 }
 
+// Low 32 bits of (hi:lo) >> s, s < 64.
+__device__ __forceinline__ uint32_t window32(uint32_t lo, uint32_t hi, uint32_t s) {
+  return s < 32 ? __funnelshift_r(lo, hi, s) : hi >> (s - 32);
+}
+
+// route_runs for two planes under the same high bits (the octal digit's
+// middle and low bits): one byte of h, its popcount and masks per chunk
+// serve both, the runs are read through 32-bit windows.
+template <uint32_t kChunks>
+__device__ __forceinline__ void route_two(uint8_t const* lut, uint64_t h, uint64_t a0,
+                                          uint64_t a1, uint64_t b0, uint64_t b1,
+                                          uint64_t& ra, uint64_t& rb) {
+  uint32_t const a0l = static_cast<uint32_t>(a0), a0h = static_cast<uint32_t>(a0 >> 32);
+  uint32_t const a1l = static_cast<uint32_t>(a1), a1h = static_cast<uint32_t>(a1 >> 32);
+  uint32_t const b0l = static_cast<uint32_t>(b0), b0h = static_cast<uint32_t>(b0 >> 32);
+  uint32_t const b1l = static_cast<uint32_t>(b1), b1h = static_cast<uint32_t>(b1 >> 32);
+  uint32_t Z = 0, O = 0;
+  uint32_t oa[2] = {0, 0}, ob[2] = {0, 0};
+#pragma unroll
+  for (uint32_t i = 0; i < kChunks; ++i) {
+    uint32_t const hb = (static_cast<uint32_t>(h >> (8 * i))) & 0xFFu;
+    uint32_t const o = __popc(hb), z = 8 - o;
+    uint32_t const mz = (1u << z) - 1u, mo = (1u << o) - 1u;
+    uint32_t const va = (window32(a0l, a0h, Z) & mz) | ((window32(a1l, a1h, O) & mo) << z);
+    uint32_t const vb = (window32(b0l, b0h, Z) & mz) | ((window32(b1l, b1h, O) & mo) << z);
+    oa[i >> 2] |= uint32_t(lut[(hb << 8) | va]) << (8 * (i & 3));
+    ob[i >> 2] |= uint32_t(lut[(hb << 8) | vb]) << (8 * (i & 3));
+    Z += z;
+    O += o;
+  }
+  ra = uint64_t(oa[0]) | (uint64_t(oa[1]) << 32);
+  rb = uint64_t(ob[0]) | (uint64_t(ob[1]) << 32);
+}
+
 void make_route_lut(std::vector<uint8_t>& lut) {
   lut.assign(65536, 0);
   for (uint32_t hb = 0; hb < 256; ++hb) {
@@ -716,8 +751,10 @@ octal_level_kernel(TreeView v, uint32_t l, uint32_t const* __restrict__ hi_w,
       if (st.uniform) {
         uint64_t const ob = r1 - st.node.ones_before;
         uint64_t const q0 = p - ob, q1 = st.node.start + st.node.zeros + ob;
-        M = route_runs<6>(lut8, H, bits64(mid_w, q0), bits64(mid_w, q1)) & vm;
-        B = route_runs<6>(lut8, H, bits64(low_w, q0), bits64(low_w, q1)) & vm;
+        route_two<6>(lut8, H, bits64(mid_w, q0), bits64(mid_w, q1), bits64(low_w, q0),
+                     bits64(low_w, q1), M, B);
+        M &= vm;
+        B &= vm;
       } else {
         uint64_t const end = p + valid;
 #pragma unroll
@@ -895,7 +932,14 @@ group_samples_kernel(uint4 const* __restrict__ blocks, uint64_t const* __restric
   ecl::detail::quad_words(x, y, q);
   uint64_t const first = b * kD;
   uint32_t const valid = first < n ? static_cast<uint32_t>(min(uint64_t(kD), n - first)) : 0u;
-  uint64_t const* sbv = sb + (b / kSb) * S;
+  uint4 const* sb4 = reinterpret_cast<uint4 const*>(sb + (b / kSb) * S);
+  uint64_t sbv[S];
+#pragma unroll
+  for (uint32_t k = 0; k < S / 2; ++k) {
+    uint4 const e = sb4[k];
+    sbv[2 * k] = uint64_t(e.y) << 32 | e.x;
+    sbv[2 * k + 1] = uint64_t(e.w) << 32 | e.z;
+  }
   uint64_t before[S];
   uint32_t c[S];
   if constexpr (W == 3) {  // headers parsed once, counts from the planes
