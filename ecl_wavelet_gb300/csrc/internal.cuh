@@ -61,6 +61,7 @@ struct QuadStore {
   std::vector<ecl::detail::QuadLevel> levels;  // host copy
   DevBuf blocks, sb, ds, node_ranks, levels_d;
   uint32_t sel_shift = ecl::detail::kDefaultSelShift;
+  bool level0_built = false;  // octal level 0 written with the binary level 0
   ecl::detail::QuadView view() const;
   uint64_t bytes() const {
     return blocks.bytes() + sb.bytes() + ds.bytes() + node_ranks.bytes() +
@@ -212,6 +213,14 @@ std::vector<uint32_t> group_widths(uint32_t L);
 // null; level 0 is then built from them directly.
 void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
                 uint32_t elem_size, cudaStream_t st);
+// Octal level 0 from the minimal symbols (1- or 2-byte) before the other
+// levels exist: lays out the group levels, writes the octal level-0 blocks
+// and the binary level 0 (`level0`, its words) in one read of the symbols,
+// and reports symbols >= 2^L in err bit 0 when `check`; build_quad finishes
+// the level.
+bool octal_text_eligible(ewt_tree const& t, uint32_t elem_size);
+void build_octal_level0(ewt_tree& t, void const* sym, uint32_t elem_size,
+                        uint32_t* level0, bool check, uint32_t* err, cudaStream_t st);
 void build_quad_samples(ewt_tree& t, uint32_t shift, cudaStream_t st);
 // Dense select samples of the binary and quad levels at rate 2^shift (0:
 // none), and the tree's view updated.

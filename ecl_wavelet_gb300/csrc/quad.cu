@@ -808,7 +808,8 @@ template <class T>
 __global__ void __launch_bounds__(1024, 1)
 octal_text_kernel(T const* __restrict__ sym, uint64_t n, uint32_t L, uint64_t nsb,
                   uint64_t num_blocks, uint4* __restrict__ blocks,
-                  uint64_t* __restrict__ sb) {
+                  uint64_t* __restrict__ sb, uint32_t* __restrict__ level0,
+                  uint32_t check_hi, uint32_t* __restrict__ err) {
   constexpr uint32_t kV = 16 / sizeof(T);           // symbols per 16-byte load
   constexpr uint32_t kLoads = uint32_t(kOctSbDigits) / kV;
   constexpr uint32_t kWords = uint32_t(kOctSbDigits) / 32 + 4;
@@ -839,6 +840,7 @@ octal_text_kernel(T const* __restrict__ sym, uint64_t n, uint32_t L, uint64_t ns
   };
   uint4 nx[kPer];
   load(first, nx);
+  bool bad = false;
   for (uint64_t sbi = first; sbi < nsb; sbi += stride) {
     uint4 cx[kPer];
 #pragma unroll
@@ -849,6 +851,8 @@ octal_text_kernel(T const* __restrict__ sym, uint64_t n, uint32_t L, uint64_t ns
       uint32_t const u = t + j * kOctSbBlocks;
       if (u >= kLoads) continue;
       uint32_t const w[4] = {cx[j].x, cx[j].y, cx[j].z, cx[j].w};
+      // a minimal symbol of 2^L is below it: no bit at or above L
+      bad |= ((w[0] | w[1] | w[2] | w[3]) & check_hi) != 0;
 #pragma unroll
       for (uint32_t b = 0; b < 3; ++b) {  // plane b: bit sb0 + 2 - b
         uint32_t const sh = sb0 + 2 - b;
@@ -870,6 +874,11 @@ octal_text_kernel(T const* __restrict__ sym, uint64_t n, uint32_t L, uint64_t ns
       }
     }
     asm volatile("bar.sync %0, 512;" ::"r"(half + 1) : "memory");
+    if (level0) {  // plane 0 is level 0's bits: 672 whole words per superblock
+      uint64_t const w0 = sbi * (kOctSbDigits / 32), words = (n + 31) / 32;
+      for (uint32_t w = t; w < kOctSbDigits / 32; w += kOctSbBlocks)
+        if (w0 + w < words) level0[w0 + w] = planes[half][0][w];
+    }
     uint64_t const blk = sbi * kOctSbBlocks + t;
     bool const mine = blk < num_blocks;
     uint64_t const p = blk * kOctDigits;
@@ -909,6 +918,7 @@ octal_text_kernel(T const* __restrict__ sym, uint64_t n, uint32_t L, uint64_t ns
     out[1] = make_uint4(static_cast<uint32_t>(w2), static_cast<uint32_t>(w2 >> 32),
                         static_cast<uint32_t>(w3), static_cast<uint32_t>(w3 >> 32));
   }
+  if (bad) atomicOr(err, 1u);
 }
 
 // Dense samples of one group level from its finished blocks and scanned
@@ -1047,28 +1057,20 @@ QuadView QuadStore::view() const {
 
 bool quad_eligible(ewt_tree const& t) { return t.pow2 && t.L >= 2 && t.n >= 1; }
 
-void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
-                uint32_t elem_size, cudaStream_t st) {
+namespace {
+
+// Block, superblock-table and level layout of a tree's group levels (needs n
+// and L only); allocates the blocks and tables.
+void layout_groups(ewt_tree& t) {
   QuadStore& qs = t.quad;
-  qs.levels.clear();
-  qs.blocks.reset();
-  if (!quad_eligible(t)) return;
-  PhaseTimer pt(EWT_PHASE_QUAD, st);
-  uint32_t const L = t.L;
   uint64_t const n = t.n;
-  EWT_REQUIRE(C.size() == t.sigma + 1 && C[t.sigma] == n, EWT_ERR_CUDA,
-              "count table inconsistent");
-  std::vector<uint32_t> const widths = group_widths(L);
-  // host: layout, digit totals, node ranks
-  std::vector<uint64_t> nr;
-  uint64_t blk = 0, sbw = 0, max_info = 0;
-  bool any_octal = false;
-  qs.levels.resize(widths.size());
+  std::vector<uint32_t> const widths = group_widths(t.L);
+  uint64_t blk = 0, sbw = 0;
+  qs.levels.assign(widths.size(), QuadLevel{});
   uint32_t l = 0;
   for (size_t j = 0; j < widths.size(); ++j) {
-    uint32_t const w = widths[j], S = 1u << w;
+    uint32_t const w = widths[j];
     QuadLevel& ql = qs.levels[j];
-    ql = QuadLevel{};
     ql.width = w;
     ql.start = l;
     uint32_t const kD = w == 3 ? kOctDigits : kQuadDigits;
@@ -1076,11 +1078,80 @@ void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
     ql.num_blocks = n / kD + 1;
     ql.blk_off = blk;
     ql.sb_off = sbw;
-    ql.nr_off = nr.size();
     blk += ql.num_blocks;
-    uint64_t const nsb = ceil_div(ql.num_blocks, uint64_t(kSb));
-    sbw += (nsb + 1) * S;  // + the totals entry
-    max_info = std::max(max_info, nsb);
+    sbw += (ceil_div(ql.num_blocks, uint64_t(kSb)) + 1) << w;  // + the totals entry
+    l += w;
+  }
+  qs.blocks.alloc(blk * 32);
+  qs.sb.alloc(sbw * 8);
+}
+
+void launch_octal_text(ewt_tree& t, void const* sym, uint32_t elem_size,
+                       uint32_t* level0, bool check, uint32_t* err, cudaStream_t st) {
+  QuadStore& qs = t.quad;
+  QuadLevel const& ql = qs.levels[0];
+  uint64_t const n = t.n;
+  uint64_t const nsb = ceil_div(ql.num_blocks, uint64_t(kOctSbBlocks));
+  uint64_t* const sb = qs.sb.as<uint64_t>() + ql.sb_off;
+  uint4* const blocks = qs.blocks.as<uint4>() + ql.blk_off * 2;
+  uint32_t const grid =
+      static_cast<uint32_t>(std::min<uint64_t>(ceil_div(nsb, 2), uint64_t(sm_count())));
+  uint32_t const lanes = elem_size == 1 ? 0x01010101u : 0x00010001u;
+  uint32_t const all = elem_size == 1 ? 0xFFu : 0xFFFFu;
+  uint32_t const check_hi = check ? lanes * ((all << t.L) & all) : 0u;
+  EWT_CUDA(cudaMemsetAsync(sb + nsb * 8, 0, 64, st));  // the totals entry
+  if (elem_size == 1)
+    octal_text_kernel<uint8_t><<<grid, 1024, 0, st>>>(
+        static_cast<uint8_t const*>(sym), n, t.L, nsb, ql.num_blocks, blocks, sb, level0,
+        check_hi, err);
+  else
+    octal_text_kernel<uint16_t><<<grid, 1024, 0, st>>>(
+        static_cast<uint16_t const*>(sym), n, t.L, nsb, ql.num_blocks, blocks, sb, level0,
+        check_hi, err);
+  EWT_LAUNCHED();
+}
+
+}  // namespace
+
+bool octal_text_eligible(ewt_tree const& t, uint32_t elem_size) {
+  return quad_eligible(t) && elem_size <= 2 && group_widths(t.L).front() == 3;
+}
+
+void build_octal_level0(ewt_tree& t, void const* sym, uint32_t elem_size,
+                        uint32_t* level0, bool check, uint32_t* err, cudaStream_t st) {
+  t.quad.level0_built = false;
+  EWT_REQUIRE(octal_text_eligible(t, elem_size), EWT_ERR_CUDA, "octal level 0 not eligible");
+  PhaseTimer pt(EWT_PHASE_FILL, st);
+  layout_groups(t);
+  launch_octal_text(t, sym, elem_size, level0, check, err, st);
+  t.quad.level0_built = true;
+}
+
+void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
+                uint32_t elem_size, cudaStream_t st) {
+  QuadStore& qs = t.quad;
+  bool const early = qs.level0_built;  // octal level 0 written with level 0
+  qs.level0_built = false;
+  if (!early) {
+    qs.levels.clear();
+    qs.blocks.reset();
+  }
+  if (!quad_eligible(t)) return;
+  PhaseTimer pt(EWT_PHASE_QUAD, st);
+  uint32_t const L = t.L;
+  uint64_t const n = t.n;
+  EWT_REQUIRE(C.size() == t.sigma + 1 && C[t.sigma] == n, EWT_ERR_CUDA,
+              "count table inconsistent");
+  if (!early) layout_groups(t);
+  // host: digit totals, node ranks
+  std::vector<uint64_t> nr;
+  uint64_t max_info = 0;
+  bool any_octal = false;
+  for (auto& ql : qs.levels) {
+    uint32_t const w = ql.width, S = 1u << w, l = ql.start;
+    uint32_t const kSb = w == 3 ? kOctSbBlocks : kQuadSbBlocks;
+    ql.nr_off = nr.size();
+    max_info = std::max(max_info, ceil_div(ql.num_blocks, uint64_t(kSb)));
     if (w == 3) {
       any_octal = true;
       max_info = std::max(max_info, ceil_div(n, kMergeSbPos));
@@ -1095,10 +1166,9 @@ void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
         run[d] += C[(pre + 1) << (sh - w)] - C[pre << (sh - w)];
       }
     for (uint32_t d = 0; d < S; ++d) ql.total[d] = run[d];
-    l += w;
   }
-  qs.blocks.alloc(blk * 32);
-  qs.sb.alloc(sbw * 8);
+  std::vector<uint32_t> widths;
+  for (auto const& ql : qs.levels) widths.push_back(ql.width);
   qs.node_ranks.alloc(nr.size() * 8);
   EWT_CUDA(cudaMemcpyAsync(qs.node_ranks.get(), nr.data(), nr.size() * 8,
                            cudaMemcpyHostToDevice, st));
@@ -1163,15 +1233,8 @@ void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
     uint64_t const nsb = ceil_div(ql.num_blocks, uint64_t(kOctSbBlocks));
     uint32_t const grid_o =
         static_cast<uint32_t>(std::min<uint64_t>(ceil_div(nsb, 2), uint64_t(sms)));
-    if (lv == 0 && sym && elem_size <= 2) {  // straight from the symbols
-      EWT_CUDA(cudaMemsetAsync(sb + nsb * 8, 0, 64, st));  // the totals entry
-      if (elem_size == 1)
-        octal_text_kernel<uint8_t><<<grid_o, 1024, 0, st>>>(
-            static_cast<uint8_t const*>(sym), n, L, nsb, ql.num_blocks, blocks, sb);
-      else
-        octal_text_kernel<uint16_t><<<grid_o, 1024, 0, st>>>(
-            static_cast<uint16_t const*>(sym), n, L, nsb, ql.num_blocks, blocks, sb);
-      EWT_LAUNCHED();
+    if (lv == 0 && (early || (sym && elem_size <= 2))) {  // from the symbols
+      if (!early) launch_octal_text(t, sym, elem_size, nullptr, false, nullptr, st);
       scan_superblocks<8>(sb, nsb + 1, chunk, st);
       continue;
     }

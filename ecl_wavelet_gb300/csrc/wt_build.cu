@@ -774,7 +774,12 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
 
   // ---- level 0 bits (with an ingested host text: written by the first pass)
   uint32_t* const words = t.rs.words.as<uint32_t>();
-  if (!ingest) {
+  t.quad.level0_built = false;
+  if (!ingest && t.pow2 && octal_text_eligible(t, sizeof(T))) {
+    // level 0 is the octal level 0's top bit plane: both in one read
+    build_octal_level0(t, sym, sizeof(T), words + t.rs.meta[0].word_off, t.is_min,
+                       err_build, st);
+  } else if (!ingest) {
     PhaseTimer pt(EWT_PHASE_FILL, st);
     uint64_t const w0 = ceil_div(t.level_bits[0], 32);
     uint32_t const blocks =
