@@ -200,7 +200,7 @@ int ewt_rs_get_device_view(const ewt_rs* rs, void* view_out,
 #define EWT_PHASE_SAMPLES 5    /* select samples                           */
 #define EWT_PHASE_QUERY 6      /* query kernels                            */
 #define EWT_PHASE_H2D 7        /* host-to-device text copy                 */
-#define EWT_PHASE_QUAD 8       /* quad query levels                        */
+#define EWT_PHASE_QUAD 8       /* group (octal / quad) query levels        */
 #define EWT_NUM_PHASES 9
 typedef struct ewt_phase_times {
   double ms[EWT_NUM_PHASES];        /* accumulated device milliseconds    */
@@ -249,9 +249,10 @@ int ewt_probe_random_reads(int gpu_index, uint64_t bytes, uint32_t depth,
 /* Rebuilds the dense select samples (query side, beside the reference-format
  * samples, which exports keep) at one entry per `rate` zeros / ones: 0 drops
  * them (select then runs the reference's sample -> L1 -> L2 search, or on
- * quad levels a search of the superblock table), else a
+ * group levels a search of the superblock table), else a
  * power of two in [32, 65536]; each entry costs 4 bytes.  Built at 256 by
- * default.  Refused (EWT_ERR_INVALID_ARGUMENT) once the device view was
+ * default.  Octal group levels (3-bit digits) of power-of-two trees sample
+ * eight times as densely (rate / 8, at least 16).  Refused (EWT_ERR_INVALID_ARGUMENT) once the device view was
  * copied out.  No reference counterpart (rank_select.cuh:44-64 fixes one
  * sample per 4096 at compile time). */
 int ewt_set_select_samples(ewt_tree* tree, uint32_t rate);
