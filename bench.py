@@ -415,12 +415,17 @@ def bench_rank_select(torch, E, dev, seed=11):
     s_gpu = np.zeros(m, dtype=np.uint64)
     rs.rank(0, 1, pos, out=r_gpu)
     rs.select(0, 1, ks, out=s_gpu)
-    a = time.perf_counter()
-    rs.rank(0, 1, pos, out=r_gpu)
-    rank_s = time.perf_counter() - a
-    a = time.perf_counter()
-    rs.select(0, 1, ks, out=s_gpu)
-    sel_s = time.perf_counter() - a
+
+    def best_of(fn, reps=3):  # host wall clock: keep the fastest of a few calls
+        best = float("inf")
+        for _ in range(reps):
+            a = time.perf_counter()
+            fn()
+            best = min(best, time.perf_counter() - a)
+        return best
+
+    rank_s = best_of(lambda: rs.rank(0, 1, pos, out=r_gpu))
+    sel_s = best_of(lambda: rs.select(0, 1, ks, out=s_gpu))
     # the same call into a freshly allocated result array (the library
     # populates its pages before the GPU writes them)
     a = time.perf_counter()
