@@ -167,7 +167,7 @@ void count_launch(uint64_t k) { g_launches.fetch_add(k, std::memory_order_relaxe
 }  // namespace ewt
 
 uint64_t ewt_tree::device_bytes() const {
-  return rs.device_bytes() + quad.bytes() + counts_d.bytes() + ranks_d.bytes() +
+  return rs.device_bytes() + groups.bytes() + counts_d.bytes() + ranks_d.bytes() +
          node_base_d.bytes() + nodes_at_level_d.bytes() + code_len_d.bytes() +
          code_bits_d.bytes() + alphabet_d.bytes() + err_d.bytes();
 }

@@ -42,8 +42,8 @@ using ecl::detail::GroupShape;
 using ecl::detail::kQuadDigits;
 using ecl::detail::kQuadSbBlocks;
 using ecl::detail::kQuadSbDigits;
-using ecl::detail::QuadLevel;
-using ecl::detail::QuadView;
+using ecl::detail::GroupLevel;
+using ecl::detail::GroupView;
 
 constexpr uint32_t kOctDigits = GroupShape<3>::kDigits;
 constexpr uint32_t kOctSbBlocks = GroupShape<3>::kSbBlocks;
@@ -289,7 +289,7 @@ void scan_superblocks(uint64_t* sb, uint64_t entries, DevBuf& chunk, cudaStream_
 // block iff that offset is below c (32-bit test; 64-bit work only then).
 template <uint32_t S>
 __device__ __forceinline__ void put_group_samples(uint32_t* __restrict__ ds,
-                                                  QuadLevel const& ql, uint64_t blk,
+                                                  GroupLevel const& ql, uint64_t blk,
                                                   uint64_t const before[S],
                                                   uint32_t const c[S]) {
   uint32_t const sh = ql.sel_shift;
@@ -380,7 +380,7 @@ __device__ __forceinline__ uint32_t group_exclusive_scan32(uint32_t x, uint32_t*
 // own superblocks (one thread per 96-digit block), the digit table shared
 // in shared memory.
 __global__ void __launch_bounds__(1024, 1)
-quad_level_kernel(TreeView v, uint32_t l, QuadLevel ql,
+quad_level_kernel(TreeView v, uint32_t l, GroupLevel ql,
                   uint32_t const* __restrict__ hi_w, uint64_t hi_words,
                   uint32_t const* __restrict__ lo_w, uint64_t lo_limit,
                   uint16_t const* __restrict__ lut_g,
@@ -926,7 +926,7 @@ octal_text_kernel(T const* __restrict__ sym, uint64_t n, uint32_t L, uint64_t ns
 template <int W>
 __global__ void __launch_bounds__(256)
 group_samples_kernel(uint4 const* __restrict__ blocks, uint64_t const* __restrict__ sb,
-                     uint64_t n, QuadLevel ql, uint32_t* __restrict__ ds,
+                     uint64_t n, GroupLevel ql, uint32_t* __restrict__ ds,
                      uint32_t* __restrict__ err) {
   constexpr uint32_t S = 1u << W;
   constexpr uint32_t kD = GroupShape<W>::kDigits, kSb = GroupShape<W>::kSbBlocks;
@@ -990,7 +990,7 @@ uint32_t level_shift(uint32_t width, uint32_t shift) {
 }
 
 // Lays out the dense samples of every group level at rate 2^shift.
-void layout_quad_samples(QuadStore& qs, uint32_t shift) {
+void layout_group_samples(GroupStore& qs, uint32_t shift) {
   qs.ds.reset();
   qs.sel_shift = shift;
   uint64_t total = 0;
@@ -1006,7 +1006,7 @@ void layout_quad_samples(QuadStore& qs, uint32_t shift) {
   if (shift) qs.ds.alloc(std::max<uint64_t>(total, 1) * 4);
 }
 
-void run_quad_samples(QuadStore& qs, uint64_t n, uint32_t* err, cudaStream_t st) {
+void run_group_samples(GroupStore& qs, uint64_t n, uint32_t* err, cudaStream_t st) {
   if (!qs.ds.get()) return;
   for (auto const& ql : qs.levels) {
     uint32_t* const ds = qs.ds.get() ? qs.ds.as<uint32_t>() : nullptr;
@@ -1021,11 +1021,11 @@ void run_quad_samples(QuadStore& qs, uint64_t n, uint32_t* err, cudaStream_t st)
   }
 }
 
-void upload_levels(QuadStore& qs, cudaStream_t st) {
-  qs.levels_d.alloc(std::max<size_t>(qs.levels.size(), 1) * sizeof(QuadLevel));
+void upload_levels(GroupStore& qs, cudaStream_t st) {
+  qs.levels_d.alloc(std::max<size_t>(qs.levels.size(), 1) * sizeof(GroupLevel));
   if (!qs.levels.empty())
     EWT_CUDA(cudaMemcpyAsync(qs.levels_d.get(), qs.levels.data(),
-                             qs.levels.size() * sizeof(QuadLevel),
+                             qs.levels.size() * sizeof(GroupLevel),
                              cudaMemcpyHostToDevice, st));
 }
 
@@ -1040,14 +1040,14 @@ std::vector<uint32_t> group_widths(uint32_t L) {
   return w;
 }
 
-QuadView QuadStore::view() const {
-  QuadView v{};
+GroupView GroupStore::view() const {
+  GroupView v{};
   if (levels.empty() || !blocks.get()) return v;
   v.blocks = blocks.as<uint4>();
   v.sb = sb.as<uint64_t>();
   v.ds = sel_shift && ds.get() ? ds.as<uint32_t>() : nullptr;
   v.node_ranks = node_ranks.as<uint64_t>();
-  v.levels = levels_d.as<QuadLevel>();
+  v.levels = levels_d.as<GroupLevel>();
   v.num = static_cast<uint32_t>(levels.size());
   uint32_t covered = 0;
   for (auto const& ql : levels) covered += ql.width;
@@ -1055,22 +1055,22 @@ QuadView QuadStore::view() const {
   return v;
 }
 
-bool quad_eligible(ewt_tree const& t) { return t.pow2 && t.L >= 2 && t.n >= 1; }
+bool groups_eligible(ewt_tree const& t) { return t.pow2 && t.L >= 2 && t.n >= 1; }
 
 namespace {
 
 // Block, superblock-table and level layout of a tree's group levels (needs n
 // and L only); allocates the blocks and tables.
 void layout_groups(ewt_tree& t) {
-  QuadStore& qs = t.quad;
+  GroupStore& qs = t.groups;
   uint64_t const n = t.n;
   std::vector<uint32_t> const widths = group_widths(t.L);
   uint64_t blk = 0, sbw = 0;
-  qs.levels.assign(widths.size(), QuadLevel{});
+  qs.levels.assign(widths.size(), GroupLevel{});
   uint32_t l = 0;
   for (size_t j = 0; j < widths.size(); ++j) {
     uint32_t const w = widths[j];
-    QuadLevel& ql = qs.levels[j];
+    GroupLevel& ql = qs.levels[j];
     ql.width = w;
     ql.start = l;
     uint32_t const kD = w == 3 ? kOctDigits : kQuadDigits;
@@ -1088,8 +1088,8 @@ void layout_groups(ewt_tree& t) {
 
 void launch_octal_text(ewt_tree& t, void const* sym, uint32_t elem_size,
                        uint32_t* level0, bool check, uint32_t* err, cudaStream_t st) {
-  QuadStore& qs = t.quad;
-  QuadLevel const& ql = qs.levels[0];
+  GroupStore& qs = t.groups;
+  GroupLevel const& ql = qs.levels[0];
   uint64_t const n = t.n;
   uint64_t const nsb = ceil_div(ql.num_blocks, uint64_t(kOctSbBlocks));
   uint64_t* const sb = qs.sb.as<uint64_t>() + ql.sb_off;
@@ -1114,29 +1114,29 @@ void launch_octal_text(ewt_tree& t, void const* sym, uint32_t elem_size,
 }  // namespace
 
 bool octal_text_eligible(ewt_tree const& t, uint32_t elem_size) {
-  return quad_eligible(t) && elem_size <= 2 && group_widths(t.L).front() == 3;
+  return groups_eligible(t) && elem_size <= 2 && group_widths(t.L).front() == 3;
 }
 
 void build_octal_level0(ewt_tree& t, void const* sym, uint32_t elem_size,
                         uint32_t* level0, bool check, uint32_t* err, cudaStream_t st) {
-  t.quad.level0_built = false;
+  t.groups.level0_built = false;
   EWT_REQUIRE(octal_text_eligible(t, elem_size), EWT_ERR_CUDA, "octal level 0 not eligible");
   PhaseTimer pt(EWT_PHASE_FILL, st);
   layout_groups(t);
   launch_octal_text(t, sym, elem_size, level0, check, err, st);
-  t.quad.level0_built = true;
+  t.groups.level0_built = true;
 }
 
-void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
+void build_groups(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
                 uint32_t elem_size, cudaStream_t st) {
-  QuadStore& qs = t.quad;
+  GroupStore& qs = t.groups;
   bool const early = qs.level0_built;  // octal level 0 written with level 0
   qs.level0_built = false;
   if (!early) {
     qs.levels.clear();
     qs.blocks.reset();
   }
-  if (!quad_eligible(t)) return;
+  if (!groups_eligible(t)) return;
   PhaseTimer pt(EWT_PHASE_QUAD, st);
   uint32_t const L = t.L;
   uint64_t const n = t.n;
@@ -1172,7 +1172,7 @@ void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
   qs.node_ranks.alloc(nr.size() * 8);
   EWT_CUDA(cudaMemcpyAsync(qs.node_ranks.get(), nr.data(), nr.size() * 8,
                            cudaMemcpyHostToDevice, st));
-  layout_quad_samples(qs, qs.sel_shift);
+  layout_group_samples(qs, qs.sel_shift);
   upload_levels(qs, st);
   static std::vector<uint16_t> const lut = [] {
     std::vector<uint16_t> v;
@@ -1287,18 +1287,18 @@ void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
 
 void set_select_rate(ewt_tree& t, uint32_t shift, cudaStream_t st) {
   build_dense_samples(t.rs, shift, st);
-  build_quad_samples(t, shift, st);
+  build_group_samples(t, shift, st);
   t.view.rs = t.rs.view();
-  t.view.quad = t.quad.view();
+  t.view.groups = t.groups.view();
 }
 
-void build_quad_samples(ewt_tree& t, uint32_t shift, cudaStream_t st) {
-  QuadStore& qs = t.quad;
+void build_group_samples(ewt_tree& t, uint32_t shift, cudaStream_t st) {
+  GroupStore& qs = t.groups;
   if (qs.levels.empty()) return;
   EWT_CUDA(cudaStreamSynchronize(st));  // no query may read the old samples
-  layout_quad_samples(qs, shift);
+  layout_group_samples(qs, shift);
   upload_levels(qs, st);
-  run_quad_samples(qs, t.n, nullptr, st);
+  run_group_samples(qs, t.n, nullptr, st);
   EWT_CUDA(cudaStreamSynchronize(st));
 }
 

@@ -56,13 +56,13 @@ uint64_t rank_block_starts(std::vector<ArrayMeta> const& meta,
 // (shift 0 drops them: select then uses the reference-format samples).
 void build_dense_samples(RSStore& rs, uint32_t shift, cudaStream_t stream);
 
-// Quad query levels of a power-of-two tree (quad.cu).
-struct QuadStore {
-  std::vector<ecl::detail::QuadLevel> levels;  // host copy
+// Group (octal / quad) query levels of a power-of-two tree (groups.cu).
+struct GroupStore {
+  std::vector<ecl::detail::GroupLevel> levels;  // host copy
   DevBuf blocks, sb, ds, node_ranks, levels_d;
   uint32_t sel_shift = ecl::detail::kDefaultSelShift;
   bool level0_built = false;  // octal level 0 written with the binary level 0
-  ecl::detail::QuadView view() const;
+  ecl::detail::GroupView view() const;
   uint64_t bytes() const {
     return blocks.bytes() + sb.bytes() + ds.bytes() + node_ranks.bytes() +
            levels_d.bytes();
@@ -137,7 +137,7 @@ struct ewt_tree {
   std::vector<ewt::NodeInfoH> nodes;
   std::vector<uint64_t> nodes_at_level, node_base, level_bits;
   ewt::RSStore rs;
-  ewt::QuadStore quad;
+  ewt::GroupStore groups;  // octal / quad query levels (power-of-two trees)
   ewt::DevBuf counts_d, ranks_d, node_base_d, nodes_at_level_d, code_len_d,
       code_bits_d, alphabet_d, err_d;
   ecl::detail::TreeView view{};
@@ -201,28 +201,28 @@ void launch_serve_items(uint32_t elem_size, TreeView const* d_views,
                         void const* reqs, void const* items, uint32_t num_items,
                         uint32_t max_levels, uint32_t* req_err, cudaStream_t s);
 void prepare_serve_kernels(uint32_t elem_size);
-// Quad query levels (quad.cu): whether a tree gets them (power-of-two
+// Group query levels (groups.cu): whether a tree gets them (power-of-two
 // alphabet, two or more levels), their build from the finished binary levels
 // and count table C (sigma + 1 entries), and a rebuild of their dense select
 // samples at rate 2^shift (0: none).
-bool quad_eligible(ewt_tree const& t);
+bool groups_eligible(ewt_tree const& t);
 // Digit widths of the group levels of an L-level tree, top down: octal (3)
 // groups, then one or two quad (2) groups; they cover all L levels.
 std::vector<uint32_t> group_widths(uint32_t L);
 // sym: the tree's minimal symbols on the device (elem_size bytes each), or
 // null; level 0 is then built from them directly.
-void build_quad(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
+void build_groups(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
                 uint32_t elem_size, cudaStream_t st);
 // Octal level 0 from the minimal symbols (1- or 2-byte) before the other
 // levels exist: lays out the group levels, writes the octal level-0 blocks
 // and the binary level 0 (`level0`, its words) in one read of the symbols,
-// and reports symbols >= 2^L in err bit 0 when `check`; build_quad finishes
+// and reports symbols >= 2^L in err bit 0 when `check`; build_groups finishes
 // the level.
 bool octal_text_eligible(ewt_tree const& t, uint32_t elem_size);
 void build_octal_level0(ewt_tree& t, void const* sym, uint32_t elem_size,
                         uint32_t* level0, bool check, uint32_t* err, cudaStream_t st);
-void build_quad_samples(ewt_tree& t, uint32_t shift, cudaStream_t st);
-// Dense select samples of the binary and quad levels at rate 2^shift (0:
+void build_group_samples(ewt_tree& t, uint32_t shift, cudaStream_t st);
+// Dense select samples of the binary and group levels at rate 2^shift (0:
 // none), and the tree's view updated.
 void set_select_rate(ewt_tree& t, uint32_t shift, cudaStream_t st);
 // Random-access roofline: dependent random 32-byte reads per second over a

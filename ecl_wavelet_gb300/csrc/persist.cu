@@ -133,13 +133,13 @@ extern "C" int ewt_save(const ewt_tree* t, const char* path) {
     dev_to_file(f, t->counts_d.get(), t->counts_d.bytes(), stage, s);
     dev_to_file(f, t->ranks_d.get(), t->ranks_d.bytes(), stage, s);
     // group query levels (none for other alphabets)
-    f.put_vec(t->quad.levels);
-    f.put(t->quad.ds.get() ? t->quad.sel_shift : 0);
-    if (!t->quad.levels.empty()) {
-      dev_to_file(f, t->quad.blocks.get(), t->quad.blocks.bytes(), stage, s);
-      dev_to_file(f, t->quad.sb.get(), t->quad.sb.bytes(), stage, s);
-      dev_to_file(f, t->quad.ds.get(), t->quad.ds.bytes(), stage, s);
-      dev_to_file(f, t->quad.node_ranks.get(), t->quad.node_ranks.bytes(), stage, s);
+    f.put_vec(t->groups.levels);
+    f.put(t->groups.ds.get() ? t->groups.sel_shift : 0);
+    if (!t->groups.levels.empty()) {
+      dev_to_file(f, t->groups.blocks.get(), t->groups.blocks.bytes(), stage, s);
+      dev_to_file(f, t->groups.sb.get(), t->groups.sb.bytes(), stage, s);
+      dev_to_file(f, t->groups.ds.get(), t->groups.ds.bytes(), stage, s);
+      dev_to_file(f, t->groups.node_ranks.get(), t->groups.node_ranks.bytes(), stage, s);
     }
   });
 }
@@ -207,29 +207,29 @@ extern "C" int ewt_load(const char* path, int gpu_index, ewt_tree** out) {
                   EWT_ERR_INVALID_ARGUMENT, "index file is corrupt");
       file_to_dev(f, t->counts_d, stage, s, (sig + 1) * 8);
       file_to_dev(f, t->ranks_d, stage, s, big);
-      t->quad.levels = f.get_vec<ecl::detail::QuadLevel>(t->L / 2 + 1);
-      t->quad.sel_shift = static_cast<uint32_t>(f.get());
-      bool plan_ok = t->quad.levels.empty() ||
-                     (quad_eligible(*t) && (t->quad.sel_shift == 0 ||
-                                            (t->quad.sel_shift >= 5 && t->quad.sel_shift <= 16)));
-      if (!t->quad.levels.empty()) {
+      t->groups.levels = f.get_vec<ecl::detail::GroupLevel>(t->L / 2 + 1);
+      t->groups.sel_shift = static_cast<uint32_t>(f.get());
+      bool plan_ok = t->groups.levels.empty() ||
+                     (groups_eligible(*t) && (t->groups.sel_shift == 0 ||
+                                            (t->groups.sel_shift >= 5 && t->groups.sel_shift <= 16)));
+      if (!t->groups.levels.empty()) {
         std::vector<uint32_t> const widths = group_widths(t->L);
-        plan_ok = plan_ok && widths.size() == t->quad.levels.size();
+        plan_ok = plan_ok && widths.size() == t->groups.levels.size();
         uint32_t l = 0;
         for (size_t j = 0; plan_ok && j < widths.size(); ++j) {
-          auto const& ql = t->quad.levels[j];
+          auto const& ql = t->groups.levels[j];
           plan_ok = ql.width == widths[j] && ql.start == l && ql.sel_shift <= 16;
           l += widths[j];
         }
       }
       EWT_REQUIRE(plan_ok, EWT_ERR_INVALID_ARGUMENT, "index file is corrupt");
-      if (!t->quad.levels.empty()) {
-        file_to_dev(f, t->quad.blocks, stage, s, big);
-        file_to_dev(f, t->quad.sb, stage, s, big);
-        file_to_dev(f, t->quad.ds, stage, s, big);
-        file_to_dev(f, t->quad.node_ranks, stage, s, big);
-        upload(t->quad.levels_d, t->quad.levels, s);
-        if (t->quad.sel_shift == 0) t->quad.ds.reset();
+      if (!t->groups.levels.empty()) {
+        file_to_dev(f, t->groups.blocks, stage, s, big);
+        file_to_dev(f, t->groups.sb, stage, s, big);
+        file_to_dev(f, t->groups.ds, stage, s, big);
+        file_to_dev(f, t->groups.node_ranks, stage, s, big);
+        upload(t->groups.levels_d, t->groups.levels, s);
+        if (t->groups.sel_shift == 0) t->groups.ds.reset();
       }
       upload(t->rs.meta_d, t->rs.meta, s);
       upload(t->node_base_d, t->node_base, s);

@@ -774,7 +774,7 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
 
   // ---- level 0 bits (with an ingested host text: written by the first pass)
   uint32_t* const words = t.rs.words.as<uint32_t>();
-  t.quad.level0_built = false;
+  t.groups.level0_built = false;
   if (!ingest && t.pow2 && octal_text_eligible(t, sizeof(T))) {
     // level 0 is the octal level 0's top bit plane: both in one read
     build_octal_level0(t, sym, sizeof(T), words + t.rs.meta[0].word_off, t.is_min,
@@ -855,14 +855,14 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   build_rs_samples(t.rs, st);
   // binary levels that group levels cover get no rank blocks
   t.rs.skip_blocks.assign(L, 0);
-  if (quad_eligible(t)) {
+  if (groups_eligible(t)) {
     uint32_t covered = 0;
     for (uint32_t w : group_widths(L)) covered += w;
     for (uint32_t l = 0; l < covered; ++l) t.rs.skip_blocks[l] = 1;
   }
   build_rank_blocks(t.rs, st);
   v.rs = t.rs.view();
-  v.quad = ecl::detail::QuadView{};
+  v.groups = ecl::detail::GroupView{};
   uint32_t build_err = 0;
   EWT_CUDA(cudaMemcpyAsync(&build_err, err_build, 4, cudaMemcpyDeviceToHost,
                            st));
@@ -878,8 +878,8 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   t.counts.assign(c.begin(), c.begin() + sigma);
   t.occ.resize(sigma);
   for (uint64_t i = 0; i < sigma; ++i) t.occ[i] = c[i + 1] - c[i];
-  build_quad(t, c, sym, sizeof(T), st);
-  v.quad = t.quad.view();
+  build_groups(t, c, sym, sizeof(T), st);
+  v.groups = t.groups.view();
 }
 
 }  // namespace
@@ -906,7 +906,7 @@ void fill_tree_view(ewt_tree& t) {
   v.elem_size = t.elem_size;
   v.is_pow2 = t.pow2;
   v.is_min = t.is_min;
-  v.quad = t.quad.view();
+  v.groups = t.groups.view();
 }
 
 void build_tree(ewt_tree& t, const void* data, uint64_t n, int elem_size,

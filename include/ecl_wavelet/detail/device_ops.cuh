@@ -70,7 +70,7 @@ constexpr uint32_t kRankHighShift = 24;
 constexpr uint32_t kDefaultSelShift = 8;
 
 /* rb_off / ds0_off of an array without rank blocks / dense samples (binary
- * levels that quad levels cover); rank and select then use L1/L2. */
+ * levels that group levels cover); rank and select then use L1/L2. */
 constexpr uint64_t kNoBlocks = ~uint64_t(0);
 
 /* A set of bit arrays with rank/select support, all in device memory. */
@@ -116,7 +116,7 @@ constexpr uint32_t kQuadDigits = GroupShape<2>::kDigits;
 constexpr uint32_t kQuadSbBlocks = GroupShape<2>::kSbBlocks;
 constexpr uint64_t kQuadSbDigits = uint64_t(kQuadDigits) * kQuadSbBlocks;
 
-struct QuadLevel {
+struct GroupLevel {
   uint64_t blk_off;     // first block (2 uint4 each)
   uint64_t sb_off;      // first superblock-table word (2^width per superblock)
   uint64_t ds_off[8];   // first dense sample of each digit
@@ -129,12 +129,12 @@ struct QuadLevel {
   uint32_t reserved;
 };
 
-struct QuadView {
+struct GroupView {
   const uint4* blocks;
   const uint64_t* sb;
   const uint32_t* ds;          // null: select searches the superblocks
   const uint64_t* node_ranks;
-  const QuadLevel* levels;     // device array of num entries
+  const GroupLevel* levels;     // device array of num entries
   uint32_t num;                // group levels (0: the tree has none)
   uint32_t covered;            // binary levels they cover (the rest: binary)
 };
@@ -158,7 +158,7 @@ struct TreeView {
   uint32_t elem_size;
   uint32_t is_pow2;
   uint32_t is_min;
-  QuadView quad;                   // quad levels over the binary ones
+  GroupView groups;                 // group (octal / quad) levels over the binary ones
 };
 
 /* ---------------------------------------------------------------------- */
@@ -505,8 +505,8 @@ __device__ __forceinline__ uint64_t sb_pick(uint4 const e[1u << (W - 1)], uint32
 
 /* Digit at position p < n of group level ql and its occurrences before p. */
 template <int W>
-__device__ __forceinline__ uint32_t group_access(const QuadView& v,
-                                                 QuadLevel const& ql, uint64_t p,
+__device__ __forceinline__ uint32_t group_access(const GroupView& v,
+                                                 GroupLevel const& ql, uint64_t p,
                                                  uint64_t* before) {
   constexpr uint32_t kD = GroupShape<W>::kDigits, kSb = GroupShape<W>::kSbBlocks;
   constexpr uint32_t kE = 1u << (W - 1);  // uint4 per superblock entry
@@ -528,8 +528,8 @@ __device__ __forceinline__ uint32_t group_access(const QuadView& v,
 
 /* Occurrences of digit d in [0, p) of group level ql, p <= n. */
 template <int W>
-__device__ __forceinline__ uint64_t group_rank(const QuadView& v,
-                                               QuadLevel const& ql, uint64_t p,
+__device__ __forceinline__ uint64_t group_rank(const GroupView& v,
+                                               GroupLevel const& ql, uint64_t p,
                                                uint32_t d) {
   constexpr uint32_t kD = GroupShape<W>::kDigits, kSb = GroupShape<W>::kSbBlocks;
   uint64_t const blk = p / kD;
@@ -585,8 +585,8 @@ __device__ __forceinline__ uint32_t group_select_in(uint64_t const q[4],
  * search starts at the block the sample rank interpolates to and moves one
  * block at a time (throughput follows the sectors read). */
 template <int W>
-__device__ __forceinline__ uint64_t group_select(const QuadView& v,
-                                                 QuadLevel const& ql,
+__device__ __forceinline__ uint64_t group_select(const GroupView& v,
+                                                 GroupLevel const& ql,
                                                  uint32_t d, uint64_t k) {
   constexpr uint32_t kD = GroupShape<W>::kDigits, kSb = GroupShape<W>::kSbBlocks;
   constexpr uint32_t kS = 1u << W;  // superblock-table words per superblock
@@ -684,36 +684,36 @@ __device__ __forceinline__ uint64_t occurrences(const TreeView& t,
 /* The three walks over group levels (power-of-two alphabets): the same
  * descent as the binary walks below, w binary levels per step; binary levels
  * past the groups (at most one) are walked as in the binary code. */
-__device__ __forceinline__ uint64_t quad_node_rank(const TreeView& t,
-                                                   QuadLevel const& ql,
+__device__ __forceinline__ uint64_t group_node_rank(const TreeView& t,
+                                                   GroupLevel const& ql,
                                                    uint64_t g, uint32_t d) {
-  return __ldg(t.quad.node_ranks + ql.nr_off + (g << ql.width) + d);
+  return __ldg(t.groups.node_ranks + ql.nr_off + (g << ql.width) + d);
 }
 
-__device__ __forceinline__ uint64_t wt_access_quad(const TreeView& t,
+__device__ __forceinline__ uint64_t wt_access_groups(const TreeView& t,
                                                    ArrayMeta const* meta,
                                                    uint64_t const* counts,
                                                    uint64_t idx) {
   uint32_t const L = t.levels;
   uint64_t cs = 0;
-  for (uint32_t j = 0; j < t.quad.num; ++j) {
-    QuadLevel const& ql = t.quad.levels[j];
+  for (uint32_t j = 0; j < t.groups.num; ++j) {
+    GroupLevel const& ql = t.groups.levels[j];
     uint32_t const w = ql.width;
     uint32_t const sh = L - ql.start;  // log2 of the symbols under a node
     uint64_t before;
-    uint32_t const d = w == 3 ? group_access<3>(t.quad, ql, counts[cs] + idx, &before)
-                              : group_access<2>(t.quad, ql, counts[cs] + idx, &before);
-    if (j + 1 < t.quad.num || t.quad.covered < L)
-      idx = before - quad_node_rank(t, ql, cs >> sh, d);
+    uint32_t const d = w == 3 ? group_access<3>(t.groups, ql, counts[cs] + idx, &before)
+                              : group_access<2>(t.groups, ql, counts[cs] + idx, &before);
+    if (j + 1 < t.groups.num || t.groups.covered < L)
+      idx = before - group_node_rank(t, ql, cs >> sh, d);
     cs += uint64_t(d) << (sh - w);
   }
-  if (t.quad.covered < L) {  // last binary level: its bit alone
+  if (t.groups.covered < L) {  // last binary level: its bit alone
     if (rs_bit(t.rs, meta[L - 1], counts[cs] + idx)) cs += 1;
   }
   return cs;
 }
 
-__device__ __forceinline__ uint64_t wt_rank_quad(const TreeView& t,
+__device__ __forceinline__ uint64_t wt_rank_groups(const TreeView& t,
                                                  ArrayMeta const* meta,
                                                  uint64_t const* counts,
                                                  uint64_t const* ranks,
@@ -721,17 +721,17 @@ __device__ __forceinline__ uint64_t wt_rank_quad(const TreeView& t,
                                                  uint64_t c, uint64_t i) {
   uint32_t const L = t.levels;
   uint64_t cs = 0, res = i;
-  for (uint32_t j = 0; j < t.quad.num; ++j) {
-    QuadLevel const& ql = t.quad.levels[j];
+  for (uint32_t j = 0; j < t.groups.num; ++j) {
+    GroupLevel const& ql = t.groups.levels[j];
     uint32_t const w = ql.width;
     uint32_t const sh = L - ql.start;
     uint32_t const d = static_cast<uint32_t>(c >> (sh - w)) & ((1u << w) - 1u);
     uint64_t const p = counts[cs] + res;
-    res = (w == 3 ? group_rank<3>(t.quad, ql, p, d) : group_rank<2>(t.quad, ql, p, d)) -
-          quad_node_rank(t, ql, cs >> sh, d);
+    res = (w == 3 ? group_rank<3>(t.groups, ql, p, d) : group_rank<2>(t.groups, ql, p, d)) -
+          group_node_rank(t, ql, cs >> sh, d);
     cs += uint64_t(d) << (sh - w);
   }
-  if (t.quad.covered < L) {
+  if (t.groups.covered < L) {
     ArrayMeta const& m = meta[L - 1];
     uint64_t const start = cs ? ranks[node_index(t, node_base, cs, L - 1)] : 0;
     uint64_t const p = counts[cs] + res;
@@ -741,7 +741,7 @@ __device__ __forceinline__ uint64_t wt_rank_quad(const TreeView& t,
   return res;
 }
 
-__device__ __forceinline__ uint64_t wt_select_quad(const TreeView& t,
+__device__ __forceinline__ uint64_t wt_select_groups(const TreeView& t,
                                                    ArrayMeta const* meta,
                                                    uint64_t const* counts,
                                                    uint64_t const* ranks,
@@ -749,7 +749,7 @@ __device__ __forceinline__ uint64_t wt_select_quad(const TreeView& t,
                                                    uint64_t c, uint64_t k) {
   uint32_t const L = t.levels;
   uint64_t res = k;  // 1-based occurrence inside the current node
-  if (t.quad.covered < L) {
+  if (t.groups.covered < L) {
     ArrayMeta const& m = meta[L - 1];
     uint64_t const cs = c & ~uint64_t(1);
     uint64_t const z = cs ? ranks[node_index(t, node_base, cs, L - 1)] : 0;
@@ -760,15 +760,15 @@ __device__ __forceinline__ uint64_t wt_select_quad(const TreeView& t,
     if (res > m.bits) return t.n;
     res -= counts[cs];
   }
-  for (int j = int(t.quad.num) - 1; j >= 0; --j) {
-    QuadLevel const& ql = t.quad.levels[j];
+  for (int j = int(t.groups.num) - 1; j >= 0; --j) {
+    GroupLevel const& ql = t.groups.levels[j];
     uint32_t const w = ql.width;
     uint32_t const sh = L - ql.start;
     uint64_t const g = c >> sh;
     uint32_t const d = static_cast<uint32_t>(c >> (sh - w)) & ((1u << w) - 1u);
-    uint64_t const kk = quad_node_rank(t, ql, g, d) + res;
-    uint64_t const pos = w == 3 ? group_select<3>(t.quad, ql, d, kk)
-                                : group_select<2>(t.quad, ql, d, kk);
+    uint64_t const kk = group_node_rank(t, ql, g, d) + res;
+    uint64_t const pos = w == 3 ? group_select<3>(t.groups, ql, d, kk)
+                                : group_select<2>(t.groups, ql, d, kk);
     res = pos + 1 - counts[g << sh];
   }
   return res - 1;
@@ -782,7 +782,7 @@ __device__ __forceinline__ uint64_t wt_access(const TreeView& t,
                                               uint64_t const* ranks,
                                               uint64_t const* node_base,
                                               uint64_t idx) {
-  if (t.quad.num) return wt_access_quad(t, meta, counts, idx);
+  if (t.groups.num) return wt_access_groups(t, meta, counts, idx);
   uint64_t cs = 0, ce = t.sigma - 1;
   for (uint32_t l = 0; l < t.levels; ++l) {
     ArrayMeta const& m = meta[l];
@@ -816,7 +816,7 @@ __device__ __forceinline__ uint64_t wt_rank(const TreeView& t,
                                             uint64_t const* node_base,
                                             uint64_t c, uint64_t i) {
   if (occurrences(t, counts, c) == 0) return 0;
-  if (t.quad.num) return wt_rank_quad(t, meta, counts, ranks, node_base, c, i);
+  if (t.groups.num) return wt_rank_groups(t, meta, counts, ranks, node_base, c, i);
   uint64_t cs = 0, ce = t.sigma - 1, res = i;
   for (uint32_t l = 0; l < t.levels; ++l) {
     if (ce == cs) break;
@@ -847,7 +847,7 @@ __device__ __forceinline__ uint64_t wt_select(const TreeView& t,
                                               uint64_t const* node_base,
                                               uint64_t c, uint64_t k) {
   if (k == 0 || k > occurrences(t, counts, c)) return t.n;
-  if (t.quad.num) return wt_select_quad(t, meta, counts, ranks, node_base, c, k);
+  if (t.groups.num) return wt_select_groups(t, meta, counts, ranks, node_base, c, k);
   uint32_t const L = t.levels;
   uint64_t len = L, code = c;
   if (!t.is_pow2 && c >= t.codes_start) {
