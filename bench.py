@@ -71,7 +71,12 @@ def parse():
                    help="skip the standalone RankSelect comparison")
     p.add_argument("--no-large", action="store_true",
                    help="skip the uint16 large-alphabet build and queries")
-    p.add_argument("--cpu-sample", type=int, default=1 << 25)
+    p.add_argument("--cpu-sample", type=int, default=6 * GIB,
+                   help="symbols of the CPU baseline build in the main arm")
+    p.add_argument("--ref-sample", type=int, default=1 << 30,
+                   help="symbols per step of the --impl reference arm")
+    p.add_argument("--no-ref-gpu", action="store_true",
+                   help="skip timing the reference's own GPU build")
     p.add_argument("--only", default="all",
                    choices=["all", "build", "queries", "multi", "serve", "rs",
                             "large"],
@@ -152,39 +157,59 @@ def dist_setup(gpus):
     return world, rank, local
 
 
-def cpu_baseline_build(sigma, sample, steps=1):
-    """The oracle's build over a bounded sample, on the host cores."""
-    from oracle import oracle as O
-    O.build_library()
-    rng = np.random.default_rng(99)
-    text = rng.integers(0, sigma, sample, dtype=np.uint64).astype(np.uint8)
-    times = []
-    t = None
-    for _ in range(steps):
-        t0 = time.perf_counter()
-        t = O.OracleTree(text, np.arange(sigma))
-        times.append(time.perf_counter() - t0)
-    return text, t, times
-
-
-def run_reference(args, world, rank):
-    if rank != 0:
-        return
+def cpu_tree_baseline(sigma, sample, steps=1, warmup=0, queries=1 << 22,
+                      seed=99, text=None):
+    """The oracle's multithreaded build of the reference's structure (the
+    same levels, L1/L2 counts and samples) on every host core, over an iid
+    uniform uint8 text of `sample` symbols, then `queries` mixed queries
+    (40/40/20) answered by walking it, one query per loop iteration."""
     from oracle import oracle as O
     O.build_library()
     cores = int(O.lib().ewto_max_threads())
-    sample = args.cpu_sample
-    rng = np.random.default_rng(99)
-    text = rng.integers(0, args.sigma, sample, dtype=np.uint64).astype(np.uint8)
-    alphabet = np.arange(args.sigma)
-    for _ in range(args.warmup):
-        O.OracleTree(text, alphabet)
+    rng = np.random.default_rng(seed)
+    if text is None:
+        text = rng.integers(0, sigma, sample, dtype=np.uint8)
+    text = text[:sample]
+    alphabet = np.arange(sigma)
+    for _ in range(warmup):
+        O.OracleTree(text, alphabet, threads=0)
     times = []
-    for _ in range(args.steps):
+    t = None
+    for _ in range(steps):
+        t = None
         t0 = time.perf_counter()
-        O.OracleTree(text, alphabet)
+        t = O.OracleTree(text, alphabet, threads=0)
         times.append(time.perf_counter() - t0)
-    ms = 1e3 * statistics.mean(times)
+    res = {"build_s": times, "cores": cores,
+           "build_GB_s": sample / statistics.mean(times) / 1e9}
+    if queries:
+        counts = t.export("COUNTS").astype(np.int64)
+        occ = np.diff(np.append(counts, sample))
+        from tests.workloads import mixed_queries_from_counts
+        ty, idx, sy = mixed_queries_from_counts(rng, sample, occ, queries)
+        a = time.perf_counter()
+        _, st = t.mixed(ty, idx, sy)
+        res["mixed_queries_Mq_s"] = queries / (time.perf_counter() - a) / 1e6
+        assert st == 0
+        for kind, code in (("access", 0), ("rank", 1), ("select", 2)):
+            k = ty == code
+            a = time.perf_counter()
+            t.mixed(ty[k], idx[k], sy[k])
+            res[kind + "_Mq_s"] = int(k.sum()) / (time.perf_counter() - a) / 1e6
+    return res
+
+
+def run_reference(args, world, rank):
+    """The reference arm: the reference ships no CPU implementation of the
+    path, so this times the oracle's multithreaded CPU build of the
+    reference's exact structure on all host cores, on a bounded sample of
+    the same workload (iid uniform uint8 text, same sigma)."""
+    if rank != 0:
+        return
+    sample = args.ref_sample
+    r = cpu_tree_baseline(args.sigma, sample, steps=args.steps,
+                          warmup=args.warmup, queries=0)
+    ms = 1e3 * statistics.mean(r["build_s"])
     gbs = sample / (ms / 1e3) / 1e9
     line = {
         "impl": "reference", "metric": METRIC, "value": gbs,
@@ -193,18 +218,49 @@ def run_reference(args, world, rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "u8",
         "data": "synthetic: iid uniform uint8 text, seed 99",
         "config": {"workload": "wavelet-tree build, uint8 text, sigma=%d "
-                               "(bounded CPU sample of the 6*2^30 config)"
-                               % args.sigma, "n": sample,
+                               "(%d-symbol sample of the 6*2^30 config)"
+                               % (args.sigma, sample), "n": sample,
                    "sigma": args.sigma, "l2": "inputs larger than L2"},
-        "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": cores,
+        "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": r["cores"],
                          "kind": "port",
-                         "sample": "%d uint8 symbols, sigma=%d, full build "
-                                   "by the CPU restatement" % (sample,
-                                                               args.sigma)},
+                         "sample": "%d uint8 symbols, sigma=%d: full build of "
+                                   "the reference's structure by the "
+                                   "multithreaded CPU tree (parallel stable "
+                                   "partition per level, popcount L1/L2, "
+                                   "samples per L1 block)" % (sample,
+                                                              args.sigma)},
         "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
+
+
+def reference_gpu(n, sigma, m, reps=2, timeout=900):
+    """The reference's own GPU build (baseline/build_ref.sh, unmodified
+    sources) timed on this GPU: its build from pinned host memory and its
+    host access / rank / select calls on m pinned queries each, asserts live
+    (its default build) and with -DNDEBUG."""
+    script = os.path.join(REPO, "baseline", "build_ref.sh")
+    r = subprocess.run(["bash", script], capture_output=True, text=True)
+    if r.returncode != 0:
+        return {"unavailable": (r.stderr.strip().splitlines() or ["build failed"])[-1]}
+    out = {}
+    for name, key in (("ref_driver", "default_asserts_live"),
+                      ("ref_driver_ndebug", "ndebug")):
+        exe = os.path.join(REPO, "baseline", "_ref", name)
+        try:
+            p = subprocess.run([exe, "bench", str(n), "1", str(sigma), str(m),
+                                str(reps)], capture_output=True, text=True,
+                               timeout=timeout)
+        except subprocess.TimeoutExpired:
+            out[key] = {"unavailable": "timed out after %d s" % timeout}
+            continue
+        if p.returncode != 0:
+            out[key] = {"unavailable": "exit %d: %s" % (
+                p.returncode, p.stderr.strip()[-300:])}
+            continue
+        out[key] = json.loads(p.stdout.strip().splitlines()[-1])
+    return out
 
 
 def pass_plan(L):
@@ -761,6 +817,25 @@ def run_ours(args, world, rank, local):
         assert st == 0
 
     e2e_q_ms = timed(host_mixed, reps=2)
+    # the plain per-call host form (the reference's host access / rank /
+    # select batch calls): one call per type from pinned host buffers
+    h_acc = acc_idx.cpu().pin_memory().numpy().view(np.uint64)
+    h_rq = rq.cpu().pin_memory().numpy().view(tree.qdtype).reshape(-1)
+    h_sq = sq.cpu().pin_memory().numpy().view(tree.qdtype).reshape(-1)
+    h_oa = torch.empty(h_acc.size, dtype=torch.uint8).pin_memory().numpy()
+    h_or = torch.empty(h_rq.size, dtype=torch.int64).pin_memory().numpy()
+    h_os = torch.empty(h_sq.size, dtype=torch.int64).pin_memory().numpy()
+
+    def host_plain():
+        assert L_.ewt_access(tree.handle, h_acc.ctypes.data, h_acc.size,
+                             h_oa.ctypes.data) == 0
+        assert L_.ewt_rank(tree.handle, h_rq.ctypes.data, h_rq.size,
+                           h_or.ctypes.data) == 0
+        assert L_.ewt_select(tree.handle, h_sq.ctypes.data, h_sq.size,
+                             h_os.ctypes.data) == 0
+
+    host_plain_ms = timed(host_plain, reps=2)
+    del h_acc, h_rq, h_sq, h_oa, h_or, h_os
     # launch shapes picked by the library's autotuner, then the same calls
     tuning = tree.autotune(1 << 22)
     tuned_mixed_ms = timed(lambda: tree.mixed_device(
@@ -804,8 +879,11 @@ def run_ours(args, world, rank, local):
         "rank_Mq_s": rq.shape[0] / rank_ms / 1e3,
         "select_Mq_s": sq.shape[0] / sel_ms / 1e3,
         "e2e_mixed_host_Mq_s": m / e2e_q_ms / 1e3,
+        "plain_host_per_type_Mq_s": m / host_plain_ms / 1e3,
+        "batched_host_over_plain_host": host_plain_ms / e2e_q_ms,
         "ms": {"mixed": mixed_ms, "access": acc_ms, "rank": rank_ms,
-               "select": sel_ms, "e2e_mixed": e2e_q_ms},
+               "select": sel_ms, "e2e_mixed": e2e_q_ms,
+               "plain_host_per_type": host_plain_ms},
     }
     del out, o_acc, o_r, o_s, rq, sq, acc_idx, rec, types
     if args.only == "queries":
@@ -836,6 +914,9 @@ def run_ours(args, world, rank, local):
            "queries_Mq_s": queries["e2e_mixed_host_Mq_s"],
            "queries_h2d_bytes": m * 17, "queries_d2h_bytes": m * 8}
     del h_text, h_np
+    cpu_text = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu_text = text[:min(args.cpu_sample, n)].cpu().numpy()
 
     # ---- sigma sweep -------------------------------------------------------
     if not args.no_sweep:
@@ -868,26 +949,26 @@ def run_ours(args, world, rank, local):
         torch.cuda.empty_cache()
         large = bench_large_alphabet(torch, E, dev, gen)
 
+    # ---- the reference's own GPU build on this GPU (rank 0, N = 1) ---------
+    ref_gpu = None
+    if rank == 0 and world == 1 and not args.no_ref_gpu:
+        torch.cuda.empty_cache()
+        ref_gpu = reference_gpu(n, sigma, m)
+
     # ---- CPU baseline (rank 0, N = 1 only) ---------------------------------
     if rank == 0 and world == 1 and not args.no_cpu:
-        from oracle import oracle as O
-        sample = args.cpu_sample
-        _, ot, times = cpu_baseline_build(sigma, sample)
-        cores = int(O.lib().ewto_max_threads())
-        cpu = {"value": sample / times[-1] / 1e9, "unit": "GB/s",
-               "cores": cores, "kind": "port",
-               "sample": "%d uint8 symbols, sigma=%d: full build by the CPU "
-                         "restatement (level partition single-threaded, "
-                         "counts and queries on all cores)" % (sample, sigma)}
-        rng = np.random.default_rng(5)
-        qm = 1 << 21
-        ty = rng.integers(0, 3, qm).astype(np.uint8)
-        idx = rng.integers(0, sample, qm).astype(np.uint64)
-        sy = rng.integers(0, sigma, qm).astype(np.uint64)
-        idx[ty == 2] = 1 + (idx[ty == 2] % max(1, sample // sigma // 2))
-        a = time.perf_counter()
-        ot.mixed(ty, idx, sy)
-        cpu["mixed_queries_Mq_s"] = qm / (time.perf_counter() - a) / 1e6
+        sample = min(args.cpu_sample, n)
+        r = cpu_tree_baseline(sigma, sample, text=cpu_text)
+        del cpu_text
+        cpu = {"value": r["build_GB_s"], "unit": "GB/s", "cores": r["cores"],
+               "kind": "port",
+               "sample": "%d uint8 symbols, sigma=%d: one full build of the "
+                         "reference's structure by the multithreaded CPU tree "
+                         "on all host cores, then 2^22 mixed queries walked "
+                         "one per loop iteration" % (sample, sigma),
+               "mixed_queries_Mq_s": r["mixed_queries_Mq_s"],
+               "access_Mq_s": r["access_Mq_s"], "rank_Mq_s": r["rank_Mq_s"],
+               "select_Mq_s": r["select_Mq_s"]}
 
     if rank == 0:
         line = {
@@ -906,6 +987,7 @@ def run_ours(args, world, rank, local):
             "gpu_launches": launches,
             "roofline": roofline, "build": build, "queries": queries,
             "sigma_sweep_GB_s": sweep, "e2e": e2e, "cpu_baseline": cpu,
+            "reference_gpu": ref_gpu,
             "many_texts": multi, "serving": serve, "rank_select": rsel,
             "large_alphabet_u16": large,
             "clocks": clk,

@@ -121,6 +121,7 @@ SIGNATURES = {
     "ewt_rs_get_device_view": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "ewt_last_error": (C.c_char_p, []),
     "ewt_abi_version": (C.c_int, []),
+    "ewt_binary_version": (C.c_int, [C.c_int, C.POINTER(C.c_int)]),
     "ewt_release_cached_memory": (C.c_int, [C.c_int]),
     "ewt_save": (C.c_int, [C.c_void_p, C.c_char_p]),
     "ewt_load": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_void_p)]),

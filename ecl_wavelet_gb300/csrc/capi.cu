@@ -800,4 +800,12 @@ int ewt_release_cached_memory(int gpu_index) {
 }
 uint64_t ewt_launch_count(void) { return g_launches.load(); }
 
+int ewt_binary_version(int gpu_index, int* version) {
+  return guarded([&] {
+    EWT_REQUIRE(version != nullptr, EWT_ERR_INVALID_ARGUMENT, "null argument");
+    DeviceGuard g(gpu_index);
+    *version = kernel_binary_version();
+  });
+}
+
 }  // extern "C"

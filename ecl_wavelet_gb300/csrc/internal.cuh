@@ -227,6 +227,8 @@ void build_group_samples(ewt_tree& t, uint32_t shift, cudaStream_t st);
 void set_select_rate(ewt_tree& t, uint32_t shift, cudaStream_t st);
 // Random-access roofline: dependent random 32-byte reads per second over a
 // buffer of `bytes` (queries.cu).
+// binaryVersion of the mixed query kernel on the current device.
+int kernel_binary_version();
 void probe_random_reads(uint64_t bytes, uint32_t depth, uint64_t chains,
                         double* reads_per_s);
 // Times candidate launch shapes of every query kind on probe queries and

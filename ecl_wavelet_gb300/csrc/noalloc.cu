@@ -1,25 +1,31 @@
 // ewt_mixed_noalloc: the mixed access/rank/select host batch without any
 // device allocation.
 //
-// Who needs it: callers that must not allocate device memory at query time —
-// code running while a stream is being captured into a CUDA graph (where
-// cudaMalloc/cudaFree may not be called), serving loops that hand all free
-// HBM to their own arena or caching allocator at start-up, and
-// latency-critical paths where cudaFree's implicit device-wide
-// synchronisation would stall every other stream.  ewt_mixed grows
-// per-tree device scratch on demand; this entry point stages the batch in
-// a fixed array compiled into the library instead.
+// Who needs it: callers that are not allowed to allocate device memory once
+// they are running — serving loops that hand all free HBM to their own arena
+// or caching allocator at start-up (a cudaMalloc from the library would fail
+// or steal the arena's headroom), hosts that fix every component's device
+// budget in advance, and latency-critical paths where an allocation that
+// misses the pool, or cudaFree's implicit device-wide synchronisation, would
+// stall every other stream.  ewt_mixed grows per-tree device scratch on
+// demand; this entry point stages the batch in a fixed array compiled into
+// the library instead.
 //
 // The scratch is one file-scope __device__ array of kScratchBytes per GPU
 // (about 6.3 MB), present on every GPU that loads libewt.so until the
 // process exits.  Its device address is fetched once per GPU with
 // cudaGetSymbolAddress, on the first call made on that GPU, with that GPU
-// current; that first call should come before any stream capture.
+// current; that first call should come before any stream capture.  The
+// address is kept for the life of the process, so resetting a device
+// (cudaDeviceReset) after that first call is not supported.
 // All calls share the array and it keeps the last call's contents: the
 // invalid-query word is cleared on every call.  Calls are serialised by a
-// process-wide lock and each returns only after its GPU work has finished,
-// so two calls never use the array at the same time; GPU work of one call
-// that overlapped another call would race on it.
+// process-wide lock (taken before the tree's own query lock, so calls that
+// change the tree — autotuning, select-sample rates — cannot interleave) and
+// each returns only after its GPU work has finished, so two calls never use
+// the array at the same time; GPU work of one call that overlapped another
+// call would race on it.  The launch uses the tree's tuned shape and is
+// timed as a query phase, exactly as ewt_mixed's kernel.
 #include <array>
 #include <mutex>
 #include <string>
@@ -77,6 +83,7 @@ extern "C" int ewt_mixed_noalloc(ewt_tree* t, const uint8_t* types,
     EWT_REQUIRE(types && queries && results, EWT_ERR_INVALID_ARGUMENT,
                 "null type, query or result buffer");
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    std::lock_guard<std::mutex> tree_lk(t->query_mu);
     ewt::DeviceGuard g(t->device);
     unsigned char* base = scratch_on(t->device);
     uint32_t* d_err = reinterpret_cast<uint32_t*>(base);

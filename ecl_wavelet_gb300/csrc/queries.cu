@@ -281,6 +281,33 @@ rs_select_kernel(RSView v, uint32_t array, uint64_t const* __restrict__ idx,
 
 namespace {
 
+// One mixed_kernel launch with the tree's tuned shape (threads x CTAs per SM
+// when the autotuner chose them), timed as a query phase; invalid queries
+// set *err.
+template <class T>
+void launch_mixed_kernel(ewt_tree& t, uint8_t const* types, void const* in,
+                         uint64_t m, uint64_t* out, uint32_t* err,
+                         StagePlan const& p, cudaStream_t s) {
+  RelaxedCapture relaxed;
+  auto mk = mixed_kernel<T>;
+  set_smem_limit(mk, static_cast<int>(kStageLimitBytes + 4096));
+  uint32_t const threads =
+      t.tune_threads[kMixed] ? t.tune_threads[kMixed] : kQueryThreads;
+  int per_sm = 0;
+  EWT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mk, threads,
+                                                         p.bytes));
+  per_sm = std::max(per_sm, 1);
+  if (t.tune_blocks[kMixed]) per_sm = std::min<int>(per_sm, t.tune_blocks[kMixed]);
+  uint64_t const chunks = ceil_div(m, kMixChunk);
+  uint32_t const blocks = static_cast<uint32_t>(
+      std::min<uint64_t>(chunks, uint64_t(per_sm) * sm_count()));
+  PhaseTimer pt(EWT_PHASE_QUERY, s);
+  mk<<<blocks, threads, p.bytes, s>>>(t.view, types,
+                                      static_cast<QueryRec<T> const*>(in), m,
+                                      out, err, p.stage_counts, p.stage_ranks);
+  EWT_LAUNCHED();
+}
+
 template <class T, int K>
 void launch_typed(ewt_tree& t, uint8_t const* types, void const* in,
                   uint64_t m, void* out, cudaStream_t s) {
@@ -295,23 +322,8 @@ void launch_typed(ewt_tree& t, uint8_t const* types, void const* in,
   StagePlan const p = plan_stage(t);
   RelaxedCapture relaxed;  // these launches may be captured into a graph
   if (K == kMixed) {
-    auto mk = mixed_kernel<T>;
-    set_smem_limit(mk, static_cast<int>(kStageLimitBytes + 4096));
-    uint32_t const threads = t.tune_threads[K] ? t.tune_threads[K] : kQueryThreads;
-    int per_sm = 0;
-    EWT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mk,
-                                                           threads, p.bytes));
-    per_sm = std::max(per_sm, 1);
-    if (t.tune_blocks[K]) per_sm = std::min<int>(per_sm, t.tune_blocks[K]);
-    uint64_t const chunks = ceil_div(m, kMixChunk);
-    uint32_t const blocks = static_cast<uint32_t>(
-        std::min<uint64_t>(chunks, uint64_t(per_sm) * sm_count()));
-    PhaseTimer pt(EWT_PHASE_QUERY, s);
-    mk<<<blocks, threads, p.bytes, s>>>(
-        t.view, types, static_cast<QueryRec<T> const*>(in), m,
-        static_cast<uint64_t*>(out), t.err_d.as<uint32_t>(), p.stage_counts,
-        p.stage_ranks);
-    EWT_LAUNCHED();
+    launch_mixed_kernel<T>(t, types, in, m, static_cast<uint64_t*>(out),
+                           t.err_d.as<uint32_t>(), p, s);
     return;
   }
   auto k = query_kernel<T, K>;
@@ -373,20 +385,7 @@ template <class T>
 void launch_mixed_raw_typed(ewt_tree& t, uint8_t const* d_types,
                             void const* d_q, uint64_t m, uint64_t* d_out,
                             uint32_t* d_err, cudaStream_t s) {
-  StagePlan const p = plan_stage(t);
-  auto mk = mixed_kernel<T>;
-  EWT_CUDA(cudaFuncSetAttribute(mk, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(kStageLimitBytes + 4096)));
-  int per_sm = 0;
-  EWT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mk,
-                                                         kQueryThreads, p.bytes));
-  per_sm = std::max(per_sm, 1);
-  uint32_t const blocks = static_cast<uint32_t>(std::min<uint64_t>(
-      ceil_div(m, kMixChunk), uint64_t(per_sm) * sm_count()));
-  mk<<<blocks, kQueryThreads, p.bytes, s>>>(
-      t.view, d_types, static_cast<QueryRec<T> const*>(d_q), m, d_out, d_err,
-      p.stage_counts, p.stage_ranks);
-  EWT_LAUNCHED();
+  launch_mixed_kernel<T>(t, d_types, d_q, m, d_out, d_err, plan_stage(t), s);
 }
 }  // namespace
 
@@ -434,6 +433,12 @@ random_chain_kernel(uint4 const* __restrict__ a, uint64_t units, uint32_t depth,
 }
 
 }  // namespace
+
+int kernel_binary_version() {
+  cudaFuncAttributes a{};
+  EWT_CUDA(cudaFuncGetAttributes(&a, mixed_kernel<uint8_t>));
+  return a.binaryVersion;
+}
 
 void probe_random_reads(uint64_t bytes, uint32_t depth, uint64_t chains,
                         double* reads_per_s) {

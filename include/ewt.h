@@ -152,14 +152,15 @@ int ewt_query_status(ewt_tree* tree, void* stream);
 
 /* ---- allocation-free mixed batch (no counterpart in the reference) ------
  * Same inputs, results and statuses as ewt_mixed, for callers that must not
- * allocate device memory while querying: code running while a stream is
- * captured into a CUDA graph, serving loops whose arena or caching
- * allocator owns all free HBM, and latency-critical paths where cudaFree's
- * device-wide synchronisation would stall other streams.  The batch is
- * staged in a fixed array compiled into libewt.so (about 6.3 MB on every
- * GPU that loads it, held until exit); at most 262144 queries per call,
- * larger batches return EWT_ERR_TOO_LARGE without touching the GPU.  The
- * first call on a GPU looks up that array's device address; make it before
+ * allocate device memory while querying: serving loops whose arena or
+ * caching allocator owns all free HBM, hosts that fix each component's
+ * device budget up front, and latency-critical paths where an allocation or
+ * cudaFree's device-wide synchronisation would stall other streams.  The
+ * batch is staged in a fixed array compiled into libewt.so (about 6.3 MB on
+ * every GPU that loads it, held until exit); at most 262144 queries per
+ * call, larger batches return EWT_ERR_TOO_LARGE without touching the GPU.
+ * The first call on a GPU looks up that array's device address (kept for
+ * the process; a later cudaDeviceReset is not supported); make it before
  * any stream capture.  Calls share the array and are serialised; each
  * returns after its GPU work is done.                                      */
 int ewt_mixed_noalloc(ewt_tree* tree, const uint8_t* types,
@@ -215,6 +216,10 @@ const char* ewt_last_error(void); /* message of the calling thread's last
 int ewt_abi_version(void);
 /* Number of kernel launches this library issued since load (all threads). */
 uint64_t ewt_launch_count(void);
+/* SM version (major * 10 + minor, e.g. 103) of the library code that runs
+ * on GPU gpu_index, as the CUDA runtime reports it for the query kernel.
+ * No reference counterpart (diagnostic). */
+int ewt_binary_version(int gpu_index, int* version);
 
 /* ---- autotuning -----------------------------------------------------------
  * Times the query kernels on probe_queries device-generated valid queries

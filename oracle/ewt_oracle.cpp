@@ -383,29 +383,9 @@ void load_text(const void* data, uint64_t n, std::vector<uint64_t>& out) {
   for (uint64_t i = 0; i < n; ++i) out[i] = p[i];
 }
 
-int build_tree(Tree& t, const void* data, uint64_t n, int es,
-               const uint64_t* alphabet, uint64_t sigma) {
-  if (!data || n == 0) return EWT_ERR_INVALID_ARGUMENT;
-  t.n = n;
-  t.elem_size = es;
-  switch (es) {
-    case 1: load_text<uint8_t>(data, n, t.text); break;
-    case 2: load_text<uint16_t>(data, n, t.text); break;
-    case 4: load_text<uint32_t>(data, n, t.text); break;
-    case 8: load_text<uint64_t>(data, n, t.text); break;
-    default: return EWT_ERR_INVALID_ARGUMENT;
-  }
-  // wavelet_tree.cuh:590-614 alphabet detection when none is given.
-  if (sigma == 0) {
-    t.alphabet = t.text;
-    std::sort(t.alphabet.begin(), t.alphabet.end());
-    t.alphabet.erase(std::unique(t.alphabet.begin(), t.alphabet.end()),
-                     t.alphabet.end());
-  } else {
-    t.alphabet.assign(alphabet, alphabet + sigma);
-    for (uint64_t i = 1; i < sigma; ++i)
-      if (t.alphabet[i] <= t.alphabet[i - 1]) return EWT_ERR_ALPHABET;
-  }
+// Alphabet shape of a tree whose sorted alphabet is set: sigma, levels,
+// codes, node starts, nodes per level (wavelet_tree.cuh:618-724).
+int setup_shape(Tree& t) {
   t.sigma = t.alphabet.size();
   if (t.sigma < 2) return EWT_ERR_ALPHABET;  // utils.cuh:80 kMinAlphabetSize
   t.L = ceil_log2(t.sigma);
@@ -442,19 +422,13 @@ int build_tree(Tree& t, const void* data, uint64_t n, int es,
   t.node_base.assign(t.L + 1, 0);
   for (uint32_t l = 1; l <= t.L; ++l)
     t.node_base[l] = t.node_base[l - 1] + t.nodes_of(l - 1);
-  // Minimal symbols and histogram (computeGlobalHistogramKernel :170-227).
-  std::vector<uint64_t> sym(n);
-  for (uint64_t i = 0; i < n; ++i) {
-    uint64_t const m = t.to_min(t.text[i]);
-    if (m >= t.sigma) return EWT_ERR_ALPHABET;
-    sym[i] = m;
-  }
-  t.occ.assign(t.sigma, 0);
-  for (uint64_t i = 0; i < n; ++i) t.occ[sym[i]]++;
-  t.counts.assign(t.sigma, 0);
-  for (uint64_t c = 1; c < t.sigma; ++c)
-    t.counts[c] = t.counts[c - 1] + t.occ[c - 1];
-  // :776-790 level sizes: drop symbols whose code ended above level l.
+  return EWT_OK;
+}
+
+// wavelet_tree.cuh:776-790 level sizes: n minus the occurrences of the
+// symbols whose code ended above level l.
+std::vector<uint64_t> level_sizes(Tree const& t) {
+  uint64_t const n = t.n;
   std::vector<uint64_t> level_bits(t.L, n);
   if (!t.codes.empty()) {
     uint64_t const min_len = t.codes.back().len;
@@ -468,6 +442,46 @@ int build_tree(Tree& t, const void* data, uint64_t n, int es,
       if (i == 0) break;
     }
   }
+  return level_bits;
+}
+
+int build_tree(Tree& t, const void* data, uint64_t n, int es,
+               const uint64_t* alphabet, uint64_t sigma) {
+  if (!data || n == 0) return EWT_ERR_INVALID_ARGUMENT;
+  t.n = n;
+  t.elem_size = es;
+  switch (es) {
+    case 1: load_text<uint8_t>(data, n, t.text); break;
+    case 2: load_text<uint16_t>(data, n, t.text); break;
+    case 4: load_text<uint32_t>(data, n, t.text); break;
+    case 8: load_text<uint64_t>(data, n, t.text); break;
+    default: return EWT_ERR_INVALID_ARGUMENT;
+  }
+  // wavelet_tree.cuh:590-614 alphabet detection when none is given.
+  if (sigma == 0) {
+    t.alphabet = t.text;
+    std::sort(t.alphabet.begin(), t.alphabet.end());
+    t.alphabet.erase(std::unique(t.alphabet.begin(), t.alphabet.end()),
+                     t.alphabet.end());
+  } else {
+    t.alphabet.assign(alphabet, alphabet + sigma);
+    for (uint64_t i = 1; i < sigma; ++i)
+      if (t.alphabet[i] <= t.alphabet[i - 1]) return EWT_ERR_ALPHABET;
+  }
+  if (int st = setup_shape(t); st != EWT_OK) return st;
+  // Minimal symbols and histogram (computeGlobalHistogramKernel :170-227).
+  std::vector<uint64_t> sym(n);
+  for (uint64_t i = 0; i < n; ++i) {
+    uint64_t const m = t.to_min(t.text[i]);
+    if (m >= t.sigma) return EWT_ERR_ALPHABET;
+    sym[i] = m;
+  }
+  t.occ.assign(t.sigma, 0);
+  for (uint64_t i = 0; i < n; ++i) t.occ[sym[i]]++;
+  t.counts.assign(t.sigma, 0);
+  for (uint64_t c = 1; c < t.sigma; ++c)
+    t.counts[c] = t.counts[c - 1] + t.occ[c - 1];
+  std::vector<uint64_t> const level_bits = level_sizes(t);
   // :806-818 level l order = text stably sorted on the top l code bits;
   // level l stores bit L-1-l of the first level_bits[l] codes.
   std::vector<uint64_t> cur(n), nxt(n);
@@ -534,6 +548,399 @@ struct RSSet {
   std::vector<BitRS> arrays;
 };
 
+// ---- multithreaded build -------------------------------------------------
+// The same structure as build_tree, built on all host cores for texts of
+// billions of symbols: the CPU baseline of the benchmark and the independent
+// full-size checker of the GPU build.  The level order is kept as narrow
+// codes (the code type C holds L bits); each level is one parallel stable
+// partition, one parallel bit packing and a RankSelect built from per-block
+// popcounts (rank_select.cu:50-304, 412-591).  The text itself is not kept:
+// the plain-scan calls of a tree built this way are refused; full-size
+// plain-scan answers come from ewto_scan_batch over the caller's text.
+
+inline uint64_t shr(uint64_t x, uint32_t s) { return s >= 64 ? 0 : x >> s; }
+
+// Ranges [r*n/parts, (r+1)*n/parts).
+inline uint64_t part_begin(uint64_t n, uint64_t parts, uint64_t r) {
+  return static_cast<uint64_t>((static_cast<unsigned __int128>(n) * r) / parts);
+}
+
+// RankSelect of one packed array (words already hold the bits), in
+// parallel: L2 block popcounts, a two-phase scan over whole L1 blocks, and
+// the select samples found by one walk over each L1 block's words.
+void build_rs_mt(BitRS& b, int nt) {
+  uint64_t const bits = b.bits;
+  uint64_t const nw = (bits + 31) / 32;
+  if (bits % 32) b.words[nw - 1] &= (uint32_t(1) << (bits % 32)) - 1;
+  uint64_t const num_l1 = (bits + kL1Bits - 1) / kL1Bits;
+  b.num_last_l2 = ((bits % kL1Bits) + kL2Bits - 1) / kL2Bits;
+  if (b.num_last_l2 == 0) b.num_last_l2 = kL2PerL1;
+  uint64_t const num_l2 = (num_l1 - 1) * kL2PerL1 + b.num_last_l2;
+  b.l1.assign(num_l1, 0);
+  b.l2.assign(num_l2, 0);
+  // ones per L1 block
+  std::vector<uint64_t> l1_ones(num_l1, 0);
+#pragma omp parallel for schedule(static) num_threads(nt)
+  for (int64_t B = 0; B < int64_t(num_l1); ++B) {
+    uint64_t const w1 = std::min<uint64_t>((uint64_t(B) + 1) * (kL1Bits / 32), nw);
+    uint64_t const k0 = uint64_t(B) * kL2PerL1;
+    uint64_t const k1 = std::min<uint64_t>(k0 + kL2PerL1, num_l2);
+    uint64_t run = 0;
+    for (uint64_t k = k0; k < k1; ++k) {
+      b.l2[k] = static_cast<uint16_t>(run);
+      uint64_t const a = k * 16, e = std::min<uint64_t>(a + 16, w1);
+      for (uint64_t w = a; w < e; ++w) run += __builtin_popcount(b.words[w]);
+    }
+    l1_ones[B] = run;
+  }
+  uint64_t cum = 0;
+  for (uint64_t B = 0; B < num_l1; ++B) {
+    b.l1[B] = cum;
+    cum += l1_ones[B];
+  }
+  b.ones = cum;
+  uint64_t const zeros = bits - b.ones;
+  b.s1.assign(b.ones / kSampleRate, 0);
+  b.s0.assign(zeros / kSampleRate, 0);
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nt)
+  for (int64_t B = 0; B < int64_t(num_l1); ++B) {
+    uint64_t const pos0 = uint64_t(B) * kL1Bits;
+    uint64_t const blk_bits = std::min<uint64_t>(kL1Bits, bits - pos0);
+    uint64_t c1 = b.l1[B], c0 = pos0 - b.l1[B];
+    uint64_t const e1 = c1 + l1_ones[B], e0 = c0 + (blk_bits - l1_ones[B]);
+    // next thresholds: the (k+1)*4096-th one / zero
+    uint64_t t1 = (c1 / kSampleRate + 1) * kSampleRate;
+    uint64_t t0 = (c0 / kSampleRate + 1) * kSampleRate;
+    if (t1 > e1 && t0 > e0) continue;
+    uint64_t const w0 = pos0 / 32;
+    uint64_t const w1 = (pos0 + blk_bits + 31) / 32;
+    for (uint64_t w = w0; w < w1 && (t1 <= e1 || t0 <= e0); ++w) {
+      uint32_t const x = b.words[w];
+      uint32_t const valid = std::min<uint64_t>(32, bits - w * 32);
+      uint32_t const o = __builtin_popcount(x);
+      uint32_t const z = valid - o;
+      while (t1 <= c1 + o) {  // the sample's one lies in this word
+        uint32_t need = uint32_t(t1 - c1), y = x;
+        for (uint32_t r = 1; r < need; ++r) y &= y - 1;
+        b.s1[t1 / kSampleRate - 1] = w * 32 + __builtin_ctz(y);
+        t1 += kSampleRate;
+      }
+      while (t0 <= c0 + z) {
+        uint32_t need = uint32_t(t0 - c0), y = ~x;
+        if (valid < 32) y &= (uint32_t(1) << valid) - 1;
+        for (uint32_t r = 1; r < need; ++r) y &= y - 1;
+        b.s0[t0 / kSampleRate - 1] = w * 32 + __builtin_ctz(y);
+        t0 += kSampleRate;
+      }
+      c1 += o;
+      c0 += z;
+    }
+  }
+}
+
+// Zeros of bit `sh` among the first x codes of the level order, from the
+// level's bits (positions past the level size hold codes that ended above
+// this level; their bit is 0).
+inline uint64_t zeros_before(BitRS const& b, uint64_t x) {
+  if (x <= b.bits) return x - b.rank1(x);
+  return (b.bits - b.ones) + (x - b.bits);
+}
+
+// Level l+1 order from level l's: inside every node (equal top-l code
+// bits, contiguous), zeros of bit sh keep their order in front of the ones
+// (wavelet_tree.cuh:806-818).  Destinations come from zero counts: a node
+// [s, e) sends its j-th code to s + (zeros before j in the node) or, for a
+// one, to s + (zeros in the node) + (ones before j in the node).
+template <class C>
+void partition_mt(std::vector<C> const& cur, std::vector<C>& nxt, BitRS const& b,
+                  uint32_t sh, int nt) {
+  uint64_t const n = cur.size();
+  uint32_t const psh = sh + 1;
+  auto prefix = [&](uint64_t i) { return shr(cur[i], psh); };
+  uint64_t const parts = uint64_t(nt) * 8;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+  for (int64_t r = 0; r < int64_t(parts); ++r) {
+    uint64_t i = part_begin(n, parts, r);
+    uint64_t const end = part_begin(n, parts, r + 1);
+    if (i >= end) continue;
+    uint64_t z = zeros_before(b, i);
+    while (i < end) {
+      uint64_t const p = prefix(i);
+      // node bounds by binary search (the order is sorted by prefix)
+      uint64_t lo = 0, hi = i;
+      while (lo < hi) {
+        uint64_t const mid = lo + (hi - lo) / 2;
+        if (prefix(mid) < p) lo = mid + 1; else hi = mid;
+      }
+      uint64_t const s = lo;
+      lo = i + 1;
+      hi = n;
+      while (lo < hi) {
+        uint64_t const mid = lo + (hi - lo) / 2;
+        if (prefix(mid) <= p) lo = mid + 1; else hi = mid;
+      }
+      uint64_t const e = lo;
+      uint64_t const zs = zeros_before(b, s);
+      uint64_t const nz = zeros_before(b, e) - zs;
+      uint64_t const stop = std::min(e, end);
+      uint64_t const zero_base = s - zs, one_base = nz + zs;  // branch-free
+      for (uint64_t j = i; j < stop; ++j) {
+        C const c = cur[j];
+        uint64_t const bit = (c >> sh) & 1;
+        uint64_t const d0 = zero_base + z, d1 = one_base + j - z;
+        nxt[bit ? d1 : d0] = c;
+        z += bit ^ 1;
+      }
+      i = stop;
+    }
+  }
+}
+
+// Bit sh of 32 consecutive codes, LSB first.  One- and two-byte codes are
+// gathered eight or four at a time by a multiply: the masked bits sit 8
+// (16) apart and the constant's terms move bit j of the word to bit 56 + j
+// (48 + j) without two terms meeting.
+template <class C>
+inline uint32_t pack32(C const* p, uint32_t sh, uint64_t cnt) {
+  uint32_t x = 0;
+  if (sizeof(C) <= 2 && cnt == 32) {
+    for (int g = 0; g < 4; ++g) {
+      uint64_t v[2];
+      std::memcpy(v, p + g * 8, 8 * sizeof(C) > 16 ? 16 : 8 * sizeof(C));
+      if (sizeof(C) == 1) {
+        uint64_t const m = (v[0] >> sh) & 0x0101010101010101ull;
+        x |= uint32_t((m * 0x0102040810204080ull) >> 56) << (8 * g);
+      } else {
+        for (int h = 0; h < 2; ++h) {
+          uint64_t const m = (v[h] >> sh) & 0x0001000100010001ull;
+          uint64_t const k = (uint64_t(1) << 3) | (uint64_t(1) << 18) |
+                             (uint64_t(1) << 33) | (uint64_t(1) << 48);
+          x |= uint32_t((m * k) >> 48 & 0xF) << (8 * g + 4 * h);
+        }
+      }
+    }
+    return x;
+  }
+  for (uint64_t j = 0; j < cnt; ++j) x |= uint32_t((p[j] >> sh) & 1) << j;
+  return x;
+}
+
+template <class C>
+int build_levels_mt(Tree& t, std::vector<C>& cur, int nt) {
+  uint64_t const n = t.n;
+  std::vector<uint64_t> const level_bits = level_sizes(t);
+  std::vector<C> nxt;
+  if (t.L > 1) nxt.resize(n);
+  t.levels.resize(t.L);
+  for (uint32_t l = 0; l < t.L; ++l) {
+    BitRS& b = t.levels[l];
+    b.bits = level_bits[l];
+    uint64_t const nw = (b.bits + 31) / 32;
+    b.words.resize(nw);
+    uint32_t const sh = t.L - 1 - l;
+#pragma omp parallel for schedule(static) num_threads(nt)
+    for (int64_t w = 0; w < int64_t(nw); ++w) {
+      uint64_t const i0 = uint64_t(w) * 32;
+      b.words[w] = pack32(cur.data() + i0, sh, std::min<uint64_t>(32, b.bits - i0));
+    }
+  build_rs_mt(b, nt);
+    if (l + 1 == t.L) break;
+    partition_mt(cur, nxt, b, sh, nt);
+    cur.swap(nxt);
+  }
+  // :332-352 rank0 at each node start
+  t.ranks.resize(t.nodes.size());
+#pragma omp parallel for schedule(static) num_threads(nt)
+  for (int64_t i = 0; i < int64_t(t.nodes.size()); ++i)
+    t.ranks[i] = t.levels[t.nodes[i].level].rank(t.counts[t.nodes[i].start], 0);
+  return EWT_OK;
+}
+
+// Minimal symbol of a raw value (sigma when not in the alphabet).
+template <class T>
+struct MinMap {
+  std::vector<uint32_t> lut;  // 1- and 2-byte symbols
+  Tree const* t;
+  explicit MinMap(Tree const& tree) : t(&tree) {
+    if (sizeof(T) <= 2) {
+      lut.assign(size_t(1) << (8 * sizeof(T)), uint32_t(tree.sigma));
+      for (uint64_t i = 0; i < tree.sigma; ++i) lut[tree.alphabet[i]] = uint32_t(i);
+    }
+  }
+  uint64_t operator()(T v) const {
+    if (sizeof(T) <= 2) return lut[v];
+    return t->to_min(v);
+  }
+};
+
+template <class T, class C>
+int build_text_mt(Tree& t, T const* text, int nt) {
+  uint64_t const n = t.n;
+  MinMap<T> const mm(t);
+  // code of every minimal symbol
+  std::vector<C> code(t.sigma);
+  for (uint64_t c = 0; c < t.sigma; ++c) code[c] = static_cast<C>(t.code_of(c).code);
+  std::vector<C> cur(n);
+  uint64_t const parts = uint64_t(nt);
+  std::vector<std::vector<uint64_t>> hist(parts);
+  int bad = 0;
+#pragma omp parallel for schedule(static) num_threads(nt) reduction(| : bad)
+  for (int64_t r = 0; r < int64_t(parts); ++r) {
+    auto& h = hist[r];
+    h.assign(t.sigma, 0);
+    uint64_t const a = part_begin(n, parts, r), e = part_begin(n, parts, r + 1);
+    for (uint64_t i = a; i < e; ++i) {
+      uint64_t const m = mm(text[i]);
+      if (m >= t.sigma) {
+        bad = 1;
+        break;
+      }
+      h[m]++;
+      cur[i] = code[m];
+    }
+  }
+  if (bad) return EWT_ERR_ALPHABET;
+  t.occ.assign(t.sigma, 0);
+  for (auto const& h : hist)
+    for (uint64_t c = 0; c < t.sigma; ++c) t.occ[c] += h[c];
+  t.counts.assign(t.sigma, 0);
+  for (uint64_t c = 1; c < t.sigma; ++c)
+    t.counts[c] = t.counts[c - 1] + t.occ[c - 1];
+  return build_levels_mt(t, cur, nt);
+}
+
+template <class T>
+int build_tree_mt_typed(Tree& t, T const* text, uint64_t n,
+                        const uint64_t* alphabet, uint64_t sigma, int nt) {
+  if (sigma == 0) {  // detection (wavelet_tree.cuh:590-614)
+    if (sizeof(T) <= 2) {
+      std::vector<uint8_t> seen(size_t(1) << (8 * sizeof(T)), 0);
+      uint64_t const parts = uint64_t(nt);
+      std::vector<std::vector<uint8_t>> loc(parts);
+#pragma omp parallel for schedule(static) num_threads(nt)
+      for (int64_t r = 0; r < int64_t(parts); ++r) {
+        loc[r].assign(seen.size(), 0);
+        uint64_t const a = part_begin(n, parts, r), e = part_begin(n, parts, r + 1);
+        for (uint64_t i = a; i < e; ++i) loc[r][text[i]] = 1;
+      }
+      for (auto const& v : loc)
+        for (size_t i = 0; i < seen.size(); ++i) seen[i] |= v[i];
+      for (size_t i = 0; i < seen.size(); ++i)
+        if (seen[i]) t.alphabet.push_back(i);
+    } else {
+      std::vector<T> tmp(text, text + n);
+      std::sort(tmp.begin(), tmp.end());
+      tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+      t.alphabet.assign(tmp.begin(), tmp.end());
+    }
+  } else {
+    t.alphabet.assign(alphabet, alphabet + sigma);
+    for (uint64_t i = 1; i < sigma; ++i)
+      if (t.alphabet[i] <= t.alphabet[i - 1]) return EWT_ERR_ALPHABET;
+  }
+  if (int st = setup_shape(t); st != EWT_OK) return st;
+  if (t.L <= 8) return build_text_mt<T, uint8_t>(t, text, nt);
+  if (t.L <= 16) return build_text_mt<T, uint16_t>(t, text, nt);
+  if (t.L <= 32) return build_text_mt<T, uint32_t>(t, text, nt);
+  return build_text_mt<T, uint64_t>(t, text, nt);
+}
+
+// Plain-scan answers of a mixed batch straight from a 1- or 2-byte text,
+// in O(n + m log m): per-chunk symbol counts, then one walk of every chunk
+// answering the rank queries whose position and the select queries whose
+// k-th occurrence fall in it.  Symbols >= sigma are invalid.
+template <class T>
+int scan_batch(T const* text, uint64_t n, uint64_t sigma, uint8_t const* types,
+               uint64_t const* idx, uint64_t const* sym, uint64_t m,
+               uint64_t* out, int nt) {
+  size_t const V = size_t(1) << (8 * sizeof(T));
+  if (sigma > V) sigma = V;
+  uint64_t const parts = uint64_t(nt) * 2;
+  std::vector<uint64_t> before((parts + 1) * V, 0);  // [part][v]
+#pragma omp parallel for schedule(static) num_threads(nt)
+  for (int64_t r = 0; r < int64_t(parts); ++r) {
+    uint64_t* h = &before[(r + 1) * V];
+    uint64_t const a = part_begin(n, parts, r), e = part_begin(n, parts, r + 1);
+    for (uint64_t i = a; i < e; ++i) h[text[i]]++;
+  }
+  for (uint64_t r = 1; r <= parts; ++r)
+    for (size_t v = 0; v < V; ++v) before[r * V + v] += before[(r - 1) * V + v];
+  uint64_t const* total = &before[parts * V];
+  int bad = 0;
+  struct Q {
+    uint64_t key;  // position (rank) or k (select)
+    uint64_t sym;
+    uint64_t q;
+  };
+  std::vector<std::vector<Q>> rq(parts), sq(parts);
+  for (uint64_t q = 0; q < m; ++q) {
+    uint8_t const ty = types[q];
+    if (ty == EWT_Q_ACCESS) {
+      out[q] = idx[q] < n ? text[idx[q]] : 0;
+      continue;
+    }
+    if (ty > EWT_Q_SELECT || sym[q] >= sigma ||
+        (ty == EWT_Q_RANK ? idx[q] > n : idx[q] == 0)) {
+      out[q] = UINT64_MAX;
+      bad = 1;
+      continue;
+    }
+    uint64_t const c = sym[q];
+    if (ty == EWT_Q_RANK) {
+      if (idx[q] == n) {
+        out[q] = total[c];
+        continue;
+      }
+      uint64_t lo = 0, hi = parts - 1;  // the part holding position idx
+      while (lo < hi) {
+        uint64_t const mid = (lo + hi + 1) / 2;
+        if (part_begin(n, parts, mid) <= idx[q]) lo = mid; else hi = mid - 1;
+      }
+      rq[lo].push_back({idx[q], c, q});
+    } else {
+      uint64_t const k = idx[q];
+      if (k > total[c]) {
+        out[q] = n;
+        continue;
+      }
+      uint64_t r = 0;  // the part holding the k-th occurrence
+      while (before[(r + 1) * V + c] < k) ++r;
+      sq[r].push_back({k, c, q});
+    }
+  }
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+  for (int64_t r = 0; r < int64_t(parts); ++r) {
+    auto& R = rq[r];
+    auto& S = sq[r];
+    if (R.empty() && S.empty()) continue;
+    std::sort(R.begin(), R.end(), [](Q const& x, Q const& y) { return x.key < y.key; });
+    std::sort(S.begin(), S.end(), [](Q const& x, Q const& y) {
+      return x.sym != y.sym ? x.sym < y.sym : x.key < y.key;
+    });
+    std::vector<uint64_t> run(before.begin() + r * V, before.begin() + (r + 1) * V);
+    std::vector<uint64_t> ptr(V, 0), pend(V, 0);
+    for (uint64_t j = 0; j < S.size(); ++j) {
+      if (j == 0 || S[j].sym != S[j - 1].sym) ptr[S[j].sym] = j;
+      pend[S[j].sym] = j + 1;
+    }
+    uint64_t const a = part_begin(n, parts, r), e = part_begin(n, parts, r + 1);
+    uint64_t ri = 0;
+    for (uint64_t i = a; i < e; ++i) {
+      while (ri < R.size() && R[ri].key == i) {
+        out[R[ri].q] = run[R[ri].sym];
+        ++ri;
+      }
+      T const v = text[i];
+      uint64_t const cnt = ++run[v];
+      while (ptr[v] < pend[v] && S[ptr[v]].key == cnt) {
+        out[S[ptr[v]].q] = i;
+        ++ptr[v];
+      }
+    }
+  }
+  return bad ? EWT_ERR_QUERY : EWT_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -553,6 +960,44 @@ int ewto_build(const void* data, uint64_t n, int elem_size,
 }
 
 void ewto_free(void* h) { delete static_cast<Tree*>(h); }
+
+int ewto_build_mt(const void* data, uint64_t n, int elem_size,
+                  const uint64_t* alphabet, uint64_t sigma, int nthreads,
+                  void** out) {
+  if (!out || !data || n == 0) return EWT_ERR_INVALID_ARGUMENT;
+  int const nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+  auto* t = new Tree();
+  t->n = n;
+  t->elem_size = elem_size;
+  int st;
+  switch (elem_size) {
+    case 1: st = build_tree_mt_typed(*t, static_cast<const uint8_t*>(data), n, alphabet, sigma, nt); break;
+    case 2: st = build_tree_mt_typed(*t, static_cast<const uint16_t*>(data), n, alphabet, sigma, nt); break;
+    case 4: st = build_tree_mt_typed(*t, static_cast<const uint32_t*>(data), n, alphabet, sigma, nt); break;
+    case 8: st = build_tree_mt_typed(*t, static_cast<const uint64_t*>(data), n, alphabet, sigma, nt); break;
+    default: st = EWT_ERR_INVALID_ARGUMENT;
+  }
+  if (st != EWT_OK) {
+    delete t;
+    *out = nullptr;
+    return st;
+  }
+  *out = t;
+  return EWT_OK;
+}
+
+int ewto_scan_batch(const void* text, uint64_t n, int elem_size,
+                    uint64_t sigma, const uint8_t* types, const uint64_t* idx,
+                    const uint64_t* sym, uint64_t m, uint64_t* out,
+                    int nthreads) {
+  if (!text || !types || !idx || !sym || !out) return EWT_ERR_INVALID_ARGUMENT;
+  int const nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+  if (elem_size == 1)
+    return scan_batch(static_cast<const uint8_t*>(text), n, sigma, types, idx, sym, m, out, nt);
+  if (elem_size == 2)
+    return scan_batch(static_cast<const uint16_t*>(text), n, sigma, types, idx, sym, m, out, nt);
+  return EWT_ERR_UNSUPPORTED;
+}
 
 int ewto_info(void* h, ewt_info* info) {
   auto* t = static_cast<Tree*>(h);
@@ -697,6 +1142,7 @@ int ewto_mixed(void* h, const uint8_t* types, const uint64_t* idx,
 int ewto_scan_access(void* h, const uint64_t* idx, uint64_t m, uint64_t* out) {
   auto* t = static_cast<Tree*>(h);
   if (!t) return EWT_ERR_INVALID_ARGUMENT;
+  if (t->text.size() != t->n) return EWT_ERR_UNSUPPORTED;  // built by ewto_build_mt
   for (uint64_t i = 0; i < m; ++i) out[i] = idx[i] < t->n ? t->text[idx[i]] : 0;
   return EWT_OK;
 }
@@ -705,6 +1151,7 @@ int ewto_scan_rank(void* h, const uint64_t* idx, const uint64_t* sym,
                    uint64_t m, uint64_t* out) {
   auto* t = static_cast<Tree*>(h);
   if (!t) return EWT_ERR_INVALID_ARGUMENT;
+  if (t->text.size() != t->n) return EWT_ERR_UNSUPPORTED;  // built by ewto_build_mt
   int st = EWT_OK;
   for (uint64_t i = 0; i < m; ++i) {
     uint64_t const c = t->to_min(sym[i]);
@@ -724,6 +1171,7 @@ int ewto_scan_select(void* h, const uint64_t* k, const uint64_t* sym,
                      uint64_t m, uint64_t* out) {
   auto* t = static_cast<Tree*>(h);
   if (!t) return EWT_ERR_INVALID_ARGUMENT;
+  if (t->text.size() != t->n) return EWT_ERR_UNSUPPORTED;  // built by ewto_build_mt
   int st = EWT_OK;
   for (uint64_t i = 0; i < m; ++i) {
     uint64_t const c = t->to_min(sym[i]);

@@ -28,6 +28,22 @@ extern "C" {
 int ewto_build(const void* data, uint64_t n, int elem_size,
                const uint64_t* alphabet, uint64_t sigma, void** out);
 void ewto_free(void* h);
+/* The same tree built on nthreads host threads (<= 0: all OpenMP threads)
+ * without keeping the text: the CPU baseline and the full-size checker.
+ * Exports and the walk queries work as for ewto_build; the plain-scan
+ * calls return EWT_ERR_UNSUPPORTED (use ewto_scan_batch). */
+int ewto_build_mt(const void* data, uint64_t n, int elem_size,
+                  const uint64_t* alphabet, uint64_t sigma, int nthreads,
+                  void** out);
+/* Plain-scan answers of a mixed batch (types 0/1/2) straight from a 1- or
+ * 2-byte text over the minimal alphabet [0, sigma), in O(n + m log m):
+ * access = text[i] (0 past the end), rank = occurrences before i (i <= n),
+ * select = position of the k-th occurrence (n when fewer); invalid queries
+ * give UINT64_MAX and EWT_ERR_QUERY. */
+int ewto_scan_batch(const void* text, uint64_t n, int elem_size,
+                    uint64_t sigma, const uint8_t* types, const uint64_t* idx,
+                    const uint64_t* sym, uint64_t m, uint64_t* out,
+                    int nthreads);
 int ewto_info(void* h, ewt_info* info);
 int ewto_export(void* h, int component, int level, void* buf,
                 uint64_t cap_bytes, uint64_t* size_bytes);

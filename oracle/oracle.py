@@ -66,6 +66,11 @@ def lib():
         L.ewto_build.argtypes = [C.c_void_p, C.c_uint64, C.c_int, u64p,
                                  C.c_uint64, C.POINTER(C.c_void_p)]
         L.ewto_free.argtypes = [C.c_void_p]
+        L.ewto_build_mt.argtypes = [C.c_void_p, C.c_uint64, C.c_int, u64p,
+                                    C.c_uint64, C.c_int, C.POINTER(C.c_void_p)]
+        L.ewto_scan_batch.argtypes = [C.c_void_p, C.c_uint64, C.c_int,
+                                      C.c_uint64, C.POINTER(C.c_uint8), u64p,
+                                      u64p, C.c_uint64, u64p, C.c_int]
         L.ewto_info.argtypes = [C.c_void_p, C.POINTER(Info)]
         L.ewto_export.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p,
                                   C.c_uint64, u64p]
@@ -116,20 +121,29 @@ def _u64(a):
 
 
 class OracleTree:
-    """CPU restatement of ecl::WaveletTree<T> over a numpy text."""
+    """CPU restatement of ecl::WaveletTree<T> over a numpy text.
 
-    def __init__(self, text: np.ndarray, alphabet=None):
+    threads=None: the plain restatement (keeps the text; the plain-scan
+    answers work).  threads=k (0 = all cores): the multithreaded build of
+    the same structure, which keeps no text (plain-scan answers of large
+    texts come from scan_batch)."""
+
+    def __init__(self, text: np.ndarray, alphabet=None, threads=None):
         text = np.ascontiguousarray(text)
         assert text.dtype in (np.uint8, np.uint16, np.uint32, np.uint64)
-        self.text = text
+        self.text = text if threads is None else None
         h = C.c_void_p()
         if alphabet is None:
             a, s = None, 0
         else:
             self._alpha = _u64(alphabet)
             a, s = _p(self._alpha), len(self._alpha)
-        st = lib().ewto_build(text.ctypes.data, text.size, text.itemsize, a, s,
-                              C.byref(h))
+        if threads is None:
+            st = lib().ewto_build(text.ctypes.data, text.size, text.itemsize,
+                                  a, s, C.byref(h))
+        else:
+            st = lib().ewto_build_mt(text.ctypes.data, text.size,
+                                     text.itemsize, a, s, threads, C.byref(h))
         if st != 0:
             raise ValueError("oracle build failed: status %d" % st)
         self.h = h
@@ -200,6 +214,20 @@ class OracleTree:
         out = np.zeros(k.size, np.uint64)
         st = lib().ewto_scan_select(self.h, _p(k), _p(sym), k.size, _p(out))
         return out, st
+
+
+def scan_batch(text, sigma, types, idx, sym, threads=0):
+    """Plain-scan answers of a mixed batch over a 1- or 2-byte text whose
+    alphabet is [0, sigma), in O(n + m log m) on all cores: (answers,
+    status)."""
+    text = np.ascontiguousarray(text)
+    types = np.ascontiguousarray(types, dtype=np.uint8)
+    idx, sym = _u64(idx), _u64(sym)
+    out = np.zeros(idx.size, np.uint64)
+    st = lib().ewto_scan_batch(text.ctypes.data, text.size, text.itemsize,
+                               sigma, _p(types, C.c_uint8), _p(idx), _p(sym),
+                               idx.size, _p(out), threads)
+    return out, st
 
 
 class OracleRS:

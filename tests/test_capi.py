@@ -3,7 +3,6 @@ every entry point include/ewt.h declares (no compute calls here)."""
 import ctypes
 import os
 import re
-import subprocess
 
 import pytest
 
@@ -40,12 +39,16 @@ def test_python_binding_covers_header(ewt):
     assert set(declared_functions()) <= bound
 
 
-def test_library_is_sm103a_only(ewt):
-    out = subprocess.run(["cuobjdump", "--list-elf", ewt.LIB_PATH],
-                         capture_output=True, text=True)
-    if out.returncode != 0:
-        pytest.skip("cuobjdump unavailable")
-    assert "sm_103a" in out.stdout
+def test_library_builds_for_sm103a_only():
+    from ecl_wavelet_gb300 import buildlib
+    assert buildlib.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+@pytest.mark.gpu
+def test_kernels_run_as_sm103a_code(ewt):
+    v = ctypes.c_int(0)
+    assert ewt.lib().ewt_binary_version(0, ctypes.byref(v)) == 0
+    assert v.value == 103
 
 
 def test_errors_without_gpu_are_statuses(ewt):
