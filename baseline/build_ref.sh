@@ -19,8 +19,10 @@ SRC="$OUT/src"
 REF="${EWT_REFERENCE_DIR:-/root/reference}"
 if [ -d "$REF/include/ecl_wavelet" ] && [ -d "$REF/src/bitarray" ]; then
   mkdir -p "$SRC"
+  chmod -R u+w "$SRC"
   rm -rf "$SRC/include" "$SRC/src"
-  cp -r "$REF/include" "$REF/src" "$SRC/"
+  cp -rp "$REF/include" "$REF/src" "$SRC/"
+  chmod -R u+w "$SRC"
   cp "$REF/LICENSE" "$SRC/" 2>/dev/null || true
 fi
 if [ ! -f "$SRC/include/ecl_wavelet/tree/wavelet_tree.cuh" ]; then
@@ -39,17 +41,34 @@ build_variant() {  # $1 = output name, $2.. = extra flags
   local name="$1"; shift
   local obj="$OUT/obj_$name"
   mkdir -p "$obj"
+  : > "$obj/build.log"
   local pids=() objs=()
   for u in "${UNITS[@]}"; do
     local o="$obj/$(basename "$u").o"
     objs+=("$o")
-    "$NVCC" "${FLAGS[@]}" "$@" -c "$u" -o "$o" &
+    "$NVCC" "${FLAGS[@]}" "$@" -c "$u" -o "$o" >> "$obj/build.log" 2>&1 &
     pids+=($!)
   done
-  for p in "${pids[@]}"; do wait "$p"; done
+  local failed=0
+  for p in "${pids[@]}"; do wait "$p" || failed=1; done
+  if [ "$failed" = 1 ]; then
+    grep -i "error" "$obj/build.log" | head -20 >&2
+    return 1
+  fi
   "$NVCC" -gencode arch=compute_103a,code=sm_103a -rdc=true "${objs[@]}" \
     -o "$OUT/$name" -lgomp
 }
+# up to date: both binaries newer than every source, the driver and the shim
+newest=$(find "$SRC/include" "$SRC/src" "$HERE/ref_driver.cu" "$HERE/cuda13_compat.h" \
+         "$HERE/build_ref.sh" -type f -printf '%T@\n' | sort -n | tail -1)
+fresh=1
+for b in "$OUT/ref_driver" "$OUT/ref_driver_ndebug"; do
+  if [ ! -x "$b" ] || [ "$(stat -c %Y "$b")" -lt "${newest%.*}" ]; then fresh=0; fi
+done
+if [ "$fresh" = 1 ]; then
+  echo "up to date: $OUT/ref_driver and $OUT/ref_driver_ndebug"
+  exit 0
+fi
 build_variant ref_driver &
 P1=$!
 build_variant ref_driver_ndebug -DNDEBUG &
