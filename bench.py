@@ -594,6 +594,9 @@ def bench_large_alphabet(torch, E, dev, gen, n=3 * GIB, m=1 << 26):
                         sq.data_ptr(), sq.shape[0], o_s.data_ptr(), sptr)))
 
         mixed_ms = timed(mixed)
+        E.set_work_queue(False)
+        static_ms = timed(mixed)
+        E.set_work_queue(True)
         plain_ms = plain()
         assert tree.query_status(sptr) == 0
         want = out.clone()
@@ -619,6 +622,7 @@ def bench_large_alphabet(torch, E, dev, gen, n=3 * GIB, m=1 << 26):
             "build_GB_s": 2 * n / build_s / 1e9, "build_ms": build_s * 1e3,
             "queries": m,
             "batched_mixed_Mq_s": m / mixed_ms / 1e3,
+            "batched_mixed_static_stride_Mq_s": m / static_ms / 1e3,
             "plain_per_type_Mq_s": m / plain_ms / 1e3,
             "autotuned": {"shapes": {k: [v["threads"], v["blocks_per_sm"]]
                                      for k, v in tuning.items() if k in KINDS},
@@ -786,6 +790,11 @@ def run_ours(args, world, rank, local):
     mixed_ms = timed(lambda: tree.mixed_device(types.data_ptr(), rec.data_ptr(),
                                                m, out.data_ptr(), sptr))
     assert tree.query_status(sptr) == 0
+    E.set_work_queue(False)  # the same launch with fixed-stride chunks
+    static_mixed_ms = timed(lambda: tree.mixed_device(
+        types.data_ptr(), rec.data_ptr(), m, out.data_ptr(), sptr))
+    E.set_work_queue(True)
+    assert tree.query_status(sptr) == 0
     # plain per-type calls over the same queries
     sel = {t: torch.nonzero(types == t).squeeze(1) for t in (0, 1, 2)}
     acc_idx = rec[sel[0], 0].contiguous()
@@ -873,6 +882,7 @@ def run_ours(args, world, rank, local):
                       "plain_per_type_Mq_s": m / tuned_plain_ms / 1e3},
         "n_queries": m, "mix": "40/40/20 access/rank/select, interleaved",
         "batched_mixed_Mq_s": m / mixed_ms / 1e3,
+        "batched_mixed_static_stride_Mq_s": m / static_mixed_ms / 1e3,
         "plain_per_type_Mq_s": m / plain_ms / 1e3,
         "batched_over_plain": plain_ms / mixed_ms,
         "access_Mq_s": acc_idx.numel() / acc_ms / 1e3,

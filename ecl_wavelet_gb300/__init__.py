@@ -121,6 +121,14 @@ SIGNATURES = {
     "ewt_rs_get_device_view": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "ewt_last_error": (C.c_char_p, []),
     "ewt_abi_version": (C.c_int, []),
+    "ewt_bitarray_create": (C.c_int, [C.c_void_p, C.c_uint32, C.c_int,
+                                      C.c_int, C.POINTER(C.c_void_p)]),
+    "ewt_rs_build_in_place": (C.c_int, [C.c_void_p]),
+    "ewt_needed_memory": (C.c_int, [C.c_int, C.c_uint64, C.c_uint32,
+                                    C.c_uint64, C.POINTER(C.c_uint64)]),
+    "ewt_minimal_codes": (C.c_int, [C.c_uint64, C.c_void_p, C.c_void_p,
+                                    C.c_uint64, C.POINTER(C.c_uint64)]),
+    "ewt_set_work_queue": (None, [C.c_int]),
     "ewt_binary_version": (C.c_int, [C.c_int, C.POINTER(C.c_int)]),
     "ewt_release_cached_memory": (C.c_int, [C.c_int]),
     "ewt_save": (C.c_int, [C.c_void_p, C.c_char_p]),
@@ -211,6 +219,12 @@ def probe_random_reads(bytes_: int = 8 << 30, depth: int = 4,
     _check(lib().ewt_probe_random_reads(gpu_index, bytes_, depth, chains,
                                         C.byref(r)), "probe_random_reads")
     return r.value
+
+
+def set_work_queue(enable: bool):
+    """Device work queue (default) or fixed-stride chunks for batched
+    query launches (ewt_set_work_queue)."""
+    lib().ewt_set_work_queue(1 if enable else 0)
 
 
 def release_cached_memory(gpu_index: int = 0):

@@ -145,7 +145,27 @@ __global__ void mask_tails_kernel(uint32_t* words, ArrayMeta const* meta,
     words[m.word_off + m.bits / 32] &= (1u << (m.bits % 32)) - 1u;
 }
 
+// Bits past each array's end -- in its last word and in the padding words
+// up to the next 32-word boundary -- set to zero (arrays filled by callers).
+__global__ void clear_tails_kernel(uint32_t* words, ArrayMeta const* meta,
+                                   uint32_t count) {
+  uint32_t const a = blockIdx.x;
+  if (a >= count) return;
+  ArrayMeta const m = meta[a];
+  uint64_t const w = (m.bits + 31) / 32;
+  uint64_t const padded = (w + 31) / 32 * 32;
+  uint32_t const t = threadIdx.x;  // 32 threads
+  if (t == 0 && m.bits % 32)
+    words[m.word_off + m.bits / 32] &= (1u << (m.bits % 32)) - 1u;
+  if (w + t < padded) words[m.word_off + w + t] = 0u;
+}
+
 }  // namespace
+
+namespace {
+std::atomic<bool> g_work_queue{true};
+}  // namespace
+bool work_queue_enabled() { return g_work_queue.load(std::memory_order_relaxed); }
 
 namespace {
 std::atomic<bool> g_timing{false};
@@ -642,6 +662,104 @@ int ewt_rs_build(const uint32_t* words, const uint64_t* bits,
   });
 }
 
+int ewt_bitarray_create(const uint64_t* bits, uint32_t num_arrays,
+                        int init_value, int gpu_index, ewt_rs** out) {
+  return guarded([&] {
+    EWT_REQUIRE(out != nullptr, EWT_ERR_INVALID_ARGUMENT, "out is null");
+    *out = nullptr;
+    EWT_REQUIRE(bits && num_arrays > 0 && num_arrays < 256,
+                EWT_ERR_INVALID_ARGUMENT,
+                "bits must be given for 1 to 255 arrays");
+    EWT_REQUIRE(init_value == 0 || init_value == 1, EWT_ERR_INVALID_ARGUMENT,
+                "init_value must be 0 or 1");
+    std::vector<uint64_t> b(bits, bits + num_arrays);
+    for (auto x : b)
+      EWT_REQUIRE(x > 0, EWT_ERR_INVALID_ARGUMENT, "empty bit array");
+    DeviceGuard g(gpu_index);
+    auto r = std::make_unique<ewt_rs>();
+    r->device = gpu_index;
+    r->built = false;
+    EWT_CUDA(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
+    cudaStream_t const st = r->stream;
+    try {
+      AllocStream as(st);
+      r->err_d.alloc(16);
+      EWT_CUDA(cudaMemsetAsync(r->err_d.get(), 0, 16, st));
+      r->rs.layout(b);
+      EWT_CUDA(cudaMemsetAsync(r->rs.words.get(), init_value ? 0xFF : 0,
+                               r->rs.words.bytes(), st));
+      EWT_CUDA(cudaMemsetAsync(r->rs.l1.get(), 0, r->rs.l1.bytes(), st));
+      EWT_CUDA(cudaMemsetAsync(r->rs.l2.get(), 0, r->rs.l2.bytes(), st));
+      EWT_CUDA(cudaStreamSynchronize(st));
+    } catch (...) {
+      cudaStreamSynchronize(st);
+      r.reset();
+      cudaStreamDestroy(st);
+      throw;
+    }
+    *out = r.release();
+  });
+}
+
+int ewt_rs_build_in_place(ewt_rs* r) {
+  return guarded([&] {
+    EWT_REQUIRE(r != nullptr, EWT_ERR_INVALID_ARGUMENT, "rank/select is null");
+    std::lock_guard<std::mutex> lk(r->query_mu);
+    EWT_REQUIRE(!r->built, EWT_ERR_INVALID_ARGUMENT,
+                "the rank/select support of these arrays is already built");
+    DeviceGuard g(r->device);
+    // the caller's kernels that wrote the words may run on any stream
+    EWT_CUDA(cudaDeviceSynchronize());
+    cudaStream_t const st = r->stream;
+    AllocStream as(st);
+    uint32_t const count = static_cast<uint32_t>(r->rs.meta.size());
+    clear_tails_kernel<<<count, 32, 0, st>>>(r->rs.words.as<uint32_t>(),
+                                             r->rs.meta_d.as<ArrayMeta>(), count);
+    EWT_LAUNCHED();
+    build_rs_counts(r->rs, 0, count, st);
+    build_rs_samples(r->rs, st);
+    build_rank_blocks(r->rs, st);
+    EWT_CUDA(cudaStreamSynchronize(st));
+    r->built = true;
+  });
+}
+
+int ewt_needed_memory(int kind, uint64_t n, uint32_t arrays_or_elem_size,
+                      uint64_t sigma, uint64_t* bytes) {
+  return guarded([&] {
+    EWT_REQUIRE(bytes != nullptr, EWT_ERR_INVALID_ARGUMENT, "bytes is null");
+    switch (kind) {
+      case EWT_MEM_BITARRAY:
+        *bytes = rs_bytes_bound(n, arrays_or_elem_size, false);
+        return;
+      case EWT_MEM_RANKSELECT:
+        *bytes = rs_bytes_bound(n, arrays_or_elem_size, true);
+        return;
+      case EWT_MEM_TREE:
+        EWT_REQUIRE(arrays_or_elem_size == 1 || arrays_or_elem_size == 2 ||
+                        arrays_or_elem_size == 4 || arrays_or_elem_size == 8,
+                    EWT_ERR_INVALID_ARGUMENT, "elem_size must be 1, 2, 4 or 8");
+        *bytes = build_bytes_bound(n, arrays_or_elem_size, sigma);
+        return;
+    }
+    throw Error(EWT_ERR_INVALID_ARGUMENT, "unknown memory kind");
+  });
+}
+
+int ewt_minimal_codes(uint64_t sigma, uint64_t* lens, uint64_t* codes,
+                      uint64_t cap, uint64_t* count) {
+  return guarded([&] {
+    EWT_REQUIRE(sigma >= 2, EWT_ERR_INVALID_ARGUMENT, "sigma must be >= 2");
+    std::vector<uint64_t> l, c;
+    minimal_codes(sigma, l, c);
+    if (count) *count = l.size();
+    for (uint64_t i = 0; i < l.size() && i < cap; ++i) {
+      if (lens) lens[i] = l[i];
+      if (codes) codes[i] = c[i];
+    }
+  });
+}
+
 int ewt_rs_free(ewt_rs* r) {
   return guarded([&] {
     if (!r) return;
@@ -672,6 +790,10 @@ int ewt_rs_export(const ewt_rs* r, int comp, int array, void* buf,
 
 int ewt_rs_rank(ewt_rs* r, int array, int value, const uint64_t* pos,
                 uint64_t m, uint64_t* results) {
+  if (r && !r->built) {
+    set_last_error("rank/select support not built (ewt_rs_build_in_place)");
+    return EWT_ERR_INVALID_ARGUMENT;
+  }
   if (r && (array < 0 || size_t(array) >= r->rs.meta.size())) {
     set_last_error("array index out of range");
     return EWT_ERR_INVALID_ARGUMENT;
@@ -685,6 +807,10 @@ int ewt_rs_rank(ewt_rs* r, int array, int value, const uint64_t* pos,
 
 int ewt_rs_select(ewt_rs* r, int array, int value, const uint64_t* idx,
                   uint64_t m, uint64_t* results) {
+  if (r && !r->built) {
+    set_last_error("rank/select support not built (ewt_rs_build_in_place)");
+    return EWT_ERR_INVALID_ARGUMENT;
+  }
   if (r && (array < 0 || size_t(array) >= r->rs.meta.size())) {
     set_last_error("array index out of range");
     return EWT_ERR_INVALID_ARGUMENT;
@@ -799,6 +925,8 @@ int ewt_release_cached_memory(int gpu_index) {
   });
 }
 uint64_t ewt_launch_count(void) { return g_launches.load(); }
+
+void ewt_set_work_queue(int enable) { g_work_queue.store(enable != 0); }
 
 int ewt_binary_version(int gpu_index, int* version) {
   return guarded([&] {

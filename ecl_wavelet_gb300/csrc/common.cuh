@@ -238,6 +238,29 @@ void set_smem_limit(Kernel f, int bytes) {
 // the host-side launch preparation (kernel attributes, occupancy queries) of
 // a launch made while the caller captures a CUDA graph is permitted in every
 // capture mode; restores the caller's mode on exit.
+// Device work queue of one launch.  CTAs take their next chunk from a
+// counter in device memory (q[0]) instead of a fixed stride, so a CTA that
+// drew cheap chunks (mostly access and rank walks) takes more of them than
+// one that drew select-heavy chunks; the CTA that finishes last resets the
+// counter (q[1] counts finished CTAs), so the next launch that uses the same
+// pair finds it at zero.  With q == nullptr CTA b takes chunks b, b + G, ...
+// Every thread of the CTA calls both functions (they hold a barrier).
+__device__ __forceinline__ uint64_t wq_take(uint32_t* q, uint32_t* s_next,
+                                            uint64_t prev, bool first) {
+  if (q == nullptr) return first ? blockIdx.x : prev + gridDim.x;
+  if (threadIdx.x == 0) *s_next = atomicAdd(q, 1u);
+  __syncthreads();
+  return *s_next;
+}
+__device__ __forceinline__ void wq_finish(uint32_t* q) {
+  if (q == nullptr || threadIdx.x != 0) return;
+  __threadfence();
+  if (atomicAdd(q + 1, 1u) == gridDim.x - 1) {
+    q[0] = 0u;  // every CTA has made its last take
+    q[1] = 0u;
+  }
+}
+
 class RelaxedCapture {
  public:
   RelaxedCapture() { cudaThreadExchangeStreamCaptureMode(&mode_); }

@@ -115,8 +115,15 @@ struct NodeInfoH {
 
 }  // namespace ewt
 
+// Per-tree device words next to the query error word: kQueueSlots work-queue
+// counter pairs (mixed launches take the next pair in turn, so launches that
+// overlap on different streams use different pairs).
+constexpr uint32_t kQueueSlots = 256;
+constexpr size_t kTreeErrBytes = 16 + size_t(kQueueSlots) * 8;
+
 struct ewt_tree {
   int device = 0;
+  std::atomic<uint32_t> queue_next{0};  // next work-queue counter pair
   uint32_t elem_size = 1;
   // query launch shape per kind (access, rank, select, mixed) chosen by
   // ewt_autotune: threads per CTA and resident CTAs per SM (0 = default)
@@ -150,6 +157,9 @@ struct ewt_tree {
 
 struct ewt_rs {
   int device = 0;
+  // false while the arrays are being filled by the caller (ewt_bitarray_create)
+  // and the counts and samples do not exist yet
+  bool built = true;
   mutable std::atomic<bool> view_shared{false};  // as ewt_tree::view_shared
   ewt::RSStore rs;
   ewt::DevBuf err_d;
@@ -159,6 +169,16 @@ struct ewt_rs {
 };
 
 namespace ewt {
+// Batched query launches distribute their chunks through a device work
+// queue unless ewt_set_work_queue(0) switched it off (capi.cu).
+bool work_queue_enabled();
+// The next work-queue counter pair of a tree (nullptr when launches use
+// static striding).
+inline uint32_t* queue_slot(ewt_tree& t) {
+  if (!work_queue_enabled()) return nullptr;
+  uint32_t const i = t.queue_next.fetch_add(1) % kQueueSlots;
+  return t.err_d.as<uint32_t>() + 4 + 2 * i;
+}
 // Host orchestration of one tree build (wt_build.cu).
 void build_tree(ewt_tree& t, const void* data, uint64_t n, int elem_size,
                 const void* alphabet, uint64_t sigma, cudaStream_t stream);
@@ -169,6 +189,16 @@ void set_texts_synchronized(bool v);
 bool texts_synchronized();
 // Sets t.view from the tree's device buffers and shape (wt_build.cu).
 void fill_tree_view(ewt_tree& t);
+// Shortened codes (length, code) of the last symbols of a non-power-of-two
+// alphabet of sigma symbols; none for powers of two (wt_build.cu).
+void minimal_codes(uint64_t sigma, std::vector<uint64_t>& lens,
+                   std::vector<uint64_t>& codes);
+// Upper bound of the device bytes a build of n elem_size-byte symbols over
+// sigma symbols holds at its peak, the finished tree included (wt_build.cu).
+uint64_t build_bytes_bound(uint64_t n, uint32_t elem_size, uint64_t sigma);
+// Device bytes of RankSelect-supported bit arrays (words, counts, samples,
+// query-side blocks) of `arrays` arrays of `bits` bits each (rs_build.cu).
+uint64_t rs_bytes_bound(uint64_t bits, uint32_t arrays, bool with_support);
 
 // Query launches on device buffers (queries.cu).
 void launch_access(ewt_tree& t, const uint64_t* d_idx, uint64_t m,
@@ -180,7 +210,8 @@ void launch_select(ewt_tree& t, const void* d_q, uint64_t m, uint64_t* d_out,
 void launch_mixed(ewt_tree& t, const uint8_t* d_types, const void* d_q,
                   uint64_t m, uint64_t* d_out, cudaStream_t s);
 // The mixed kernel over caller-provided device buffers with an explicit
-// invalid-query word; allocates nothing and records no timing events.
+// invalid-query word (its work-queue counter pair at d_err + 16, i.e. 64
+// bytes in, zeroed by the caller); allocates nothing.
 void launch_mixed_raw(ewt_tree& t, const uint8_t* d_types, const void* d_q,
                       uint64_t m, uint64_t* d_out, uint32_t* d_err,
                       cudaStream_t s);

@@ -206,17 +206,20 @@ multi_kernel(TreeView const* __restrict__ views,
              uint32_t const* __restrict__ perm,
              uint8_t const* __restrict__ types,
              MultiRec<T> const* __restrict__ in, uint64_t* __restrict__ out,
-             uint32_t* __restrict__ err) {
+             uint32_t* __restrict__ err, uint32_t* queue) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ __align__(8) TreeView tv;
   __shared__ MultiItem it;
   __shared__ uint16_t lists[3][kMultiChunk];
   __shared__ uint32_t list_len[3];
+  __shared__ uint32_t next_item;
   uint32_t const tid = threadIdx.x, lane = tid & 31;
   uint32_t const lt = (1u << lane) - 1u;
   uint32_t const n_items = num_items_d ? *num_items_d : num_items_h;
   uint32_t bad = 0;
-  for (uint32_t w = blockIdx.x; w < n_items; w += gridDim.x) {
+  // work items from the device queue (or by a fixed stride without one)
+  for (uint64_t w = wq_take(queue, &next_item, 0, true); w < n_items;
+       w = wq_take(queue, &next_item, w, false)) {
     if (tid == 0) it = items[w];
     if (tid < 3) list_len[tid] = 0;
     __syncthreads();
@@ -296,6 +299,7 @@ multi_kernel(TreeView const* __restrict__ views,
     }
     __syncthreads();  // tv, meta and lists are reused by the next item
   }
+  wq_finish(queue);
   if (bad) atomicOr(err, 1u);
 }
 
@@ -431,7 +435,7 @@ void launch_multi_typed(TreeView const* d_views, MultiItem const* d_items,
                         uint64_t max_items, uint32_t max_levels,
                         uint32_t const* d_perm, uint8_t const* d_types,
                         void const* d_q, uint64_t* d_out, uint32_t* d_err,
-                        cudaStream_t s) {
+                        uint32_t* d_queue, cudaStream_t s) {
   size_t const smem = max_levels * sizeof(ArrayMeta) + (max_levels + 1) * 8;
   // resident CTAs per SM, looked up once per thread and level count
   thread_local int cached[65] = {};
@@ -445,7 +449,7 @@ void launch_multi_typed(TreeView const* d_views, MultiItem const* d_items,
       1, std::min<uint64_t>(max_items, uint64_t(per_sm) * sm_count())));
   multi_kernel<T><<<blocks, kMultiThreads, smem, s>>>(
       d_views, d_items, d_num_items, h_num_items, d_perm, d_types,
-      static_cast<MultiRec<T> const*>(d_q), d_out, d_err);
+      static_cast<MultiRec<T> const*>(d_q), d_out, d_err, d_queue);
   EWT_LAUNCHED();
 }
 
@@ -454,12 +458,12 @@ void launch_multi(uint32_t elem_size, TreeView const* d_views,
                   uint32_t h_num_items, uint64_t max_items, uint32_t max_levels,
                   uint32_t const* d_perm, uint8_t const* d_types,
                   void const* d_q, uint64_t* d_out, uint32_t* d_err,
-                  cudaStream_t s) {
+                  uint32_t* d_queue, cudaStream_t s) {
   switch (elem_size) {
-    case 1: launch_multi_typed<uint8_t>(d_views, d_items, d_num_items, h_num_items, max_items, max_levels, d_perm, d_types, d_q, d_out, d_err, s); break;
-    case 2: launch_multi_typed<uint16_t>(d_views, d_items, d_num_items, h_num_items, max_items, max_levels, d_perm, d_types, d_q, d_out, d_err, s); break;
-    case 4: launch_multi_typed<uint32_t>(d_views, d_items, d_num_items, h_num_items, max_items, max_levels, d_perm, d_types, d_q, d_out, d_err, s); break;
-    default: launch_multi_typed<uint64_t>(d_views, d_items, d_num_items, h_num_items, max_items, max_levels, d_perm, d_types, d_q, d_out, d_err, s); break;
+    case 1: launch_multi_typed<uint8_t>(d_views, d_items, d_num_items, h_num_items, max_items, max_levels, d_perm, d_types, d_q, d_out, d_err, d_queue, s); break;
+    case 2: launch_multi_typed<uint16_t>(d_views, d_items, d_num_items, h_num_items, max_items, max_levels, d_perm, d_types, d_q, d_out, d_err, d_queue, s); break;
+    case 4: launch_multi_typed<uint32_t>(d_views, d_items, d_num_items, h_num_items, max_items, max_levels, d_perm, d_types, d_q, d_out, d_err, d_queue, s); break;
+    default: launch_multi_typed<uint64_t>(d_views, d_items, d_num_items, h_num_items, max_items, max_levels, d_perm, d_types, d_q, d_out, d_err, d_queue, s); break;
   }
 }
 
@@ -503,8 +507,10 @@ void multi_device(ViewSet const& vs, uint32_t num_trees, uint32_t const* d_tree_
               "a multi-tree batch holds fewer than 2^32 queries");
   uint64_t const max_items = m / kMultiChunk + num_trees + 1;
   DevBuf cnt((num_trees + 1) * 4), cursor(num_trees * 8),
-      items(max_items * sizeof(MultiItem)), nitems(4), perm(std::max<uint64_t>(m, 1) * 4);
+      items(max_items * sizeof(MultiItem)), nitems(4), perm(std::max<uint64_t>(m, 1) * 4),
+      queue(8);
   EWT_CUDA(cudaMemsetAsync(cnt.get(), 0, (num_trees + 1) * 4, s));
+  EWT_CUDA(cudaMemsetAsync(queue.get(), 0, 8, s));
   uint32_t const grid = static_cast<uint32_t>(
       std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(m, 256), uint64_t(sm_count()) * 8)));
   PhaseTimer pt(EWT_PHASE_QUERY, s);
@@ -530,7 +536,8 @@ void multi_device(ViewSet const& vs, uint32_t num_trees, uint32_t const* d_tree_
   EWT_LAUNCHED();
   launch_multi(vs.elem_size, vs.views.as<TreeView>(), items.as<MultiItem>(),
                nitems.as<uint32_t>(), 0, max_items, vs.max_levels,
-               perm.as<uint32_t>(), d_types, d_q, d_out, d_err, s);
+               perm.as<uint32_t>(), d_types, d_q, d_out, d_err,
+               work_queue_enabled() ? queue.as<uint32_t>() : nullptr, s);
 }
 
 std::mutex g_multi_mu;            // host multi-tree calls share one stream
@@ -581,7 +588,7 @@ void launch_multi_items(uint32_t elem_size, TreeView const* d_views,
   if (num_items == 0) return;
   launch_multi(elem_size, d_views, static_cast<MultiItem const*>(d_items),
                nullptr, num_items, num_items, max_levels, nullptr, d_types, d_q,
-               d_out, d_err, s);
+               d_out, d_err, nullptr, s);
 }
 
 }  // namespace ewt

@@ -19,7 +19,7 @@
 // address is kept for the life of the process, so resetting a device
 // (cudaDeviceReset) after that first call is not supported.
 // All calls share the array and it keeps the last call's contents: the
-// invalid-query word is cleared on every call.  Calls are serialised by a
+// invalid-query word and the work-queue counters are cleared on every call.  Calls are serialised by a
 // process-wide lock (taken before the tree's own query lock, so calls that
 // change the tree — autotuning, select-sample rates — cannot interleave) and
 // each returns only after its GPU work has finished, so two calls never use
@@ -36,7 +36,7 @@ namespace {
 
 // Largest batch one call accepts.
 constexpr uint64_t kNoAllocMaxQueries = uint64_t(1) << 18;  // 262,144
-constexpr size_t kErrBytes = 256;  // invalid-query word, padded to 256 B
+constexpr size_t kErrBytes = 256;  // invalid-query word + queue counters
 constexpr size_t kQueryBytes = kNoAllocMaxQueries * 16;  // RankSelectQuery
 constexpr size_t kResultBytes = kNoAllocMaxQueries * 8;
 constexpr size_t kTypeBytes = kNoAllocMaxQueries;
@@ -92,7 +92,9 @@ extern "C" int ewt_mixed_noalloc(ewt_tree* t, const uint8_t* types,
     uint8_t* d_types = reinterpret_cast<uint8_t*>(d_q + kQueryBytes +
                                                   kResultBytes);
     cudaStream_t const s = t->stream;
-    EWT_CUDA(cudaMemsetAsync(d_err, 0, sizeof(uint32_t), s));
+    // the invalid-query word and the launch's work-queue counters (bytes
+    // 64..71 of the same 256-byte region) start at zero
+    EWT_CUDA(cudaMemsetAsync(d_err, 0, kErrBytes, s));
     EWT_CUDA(cudaMemcpyAsync(d_q, queries, m * 16, cudaMemcpyDefault, s));
     EWT_CUDA(cudaMemcpyAsync(d_types, types, m, cudaMemcpyDefault, s));
     ewt::launch_mixed_raw(*t, d_types, d_q, m, d_out, d_err, s);

@@ -248,8 +248,8 @@ extern "C" int ewt_load(const char* path, int gpu_index, ewt_tree** out) {
           std::memcpy(&a[i * t->elem_size], &t->alphabet[i], t->elem_size);
         upload(t->alphabet_d, a, s);
       }
-      t->err_d.alloc(16);
-      EWT_CUDA(cudaMemsetAsync(t->err_d.get(), 0, 16, s));
+      t->err_d.alloc(kTreeErrBytes);
+      EWT_CUDA(cudaMemsetAsync(t->err_d.get(), 0, kTreeErrBytes, s));
       EWT_CUDA(cudaStreamSynchronize(s));  // host vectors above leave scope
       fill_tree_view(*t);
     } catch (...) {

@@ -149,10 +149,11 @@ __global__ void __launch_bounds__(kMaxQueryThreads)
 mixed_kernel(TreeView t, uint8_t const* __restrict__ types,
              QueryRec<T> const* __restrict__ in, uint64_t m,
              uint64_t* __restrict__ out, uint32_t* __restrict__ err,
-             uint32_t stage_counts, uint32_t stage_ranks) {
+             uint32_t stage_counts, uint32_t stage_ranks, uint32_t* queue) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint16_t lists[3][kMixChunk];
   __shared__ uint32_t list_len[3];
+  __shared__ uint32_t next_chunk;
   uint32_t const L = t.levels;
   ArrayMeta* meta = reinterpret_cast<ArrayMeta*>(smem);
   uint64_t* node_base = reinterpret_cast<uint64_t*>(meta + L);
@@ -185,7 +186,8 @@ mixed_kernel(TreeView t, uint8_t const* __restrict__ types,
   uint32_t const lt = (1u << lane) - 1u;
   uint32_t bad = 0;
   uint64_t const chunks = (m + kMixChunk - 1) / kMixChunk;
-  for (uint64_t c = blockIdx.x; c < chunks; c += gridDim.x) {
+  for (uint64_t c = wq_take(queue, &next_chunk, 0, true); c < chunks;
+       c = wq_take(queue, &next_chunk, c, false)) {
     uint64_t const base = c * kMixChunk;
     if (threadIdx.x < 3) list_len[threadIdx.x] = 0;
     __syncthreads();
@@ -239,6 +241,7 @@ mixed_kernel(TreeView t, uint8_t const* __restrict__ types,
     }
     __syncthreads();  // lists are reused by the next chunk
   }
+  wq_finish(queue);
   if (bad) atomicOr(err, 1u);
 }
 
@@ -287,7 +290,8 @@ namespace {
 template <class T>
 void launch_mixed_kernel(ewt_tree& t, uint8_t const* types, void const* in,
                          uint64_t m, uint64_t* out, uint32_t* err,
-                         StagePlan const& p, cudaStream_t s) {
+                         StagePlan const& p, cudaStream_t s,
+                         uint32_t* queue) {
   RelaxedCapture relaxed;
   auto mk = mixed_kernel<T>;
   set_smem_limit(mk, static_cast<int>(kStageLimitBytes + 4096));
@@ -304,7 +308,8 @@ void launch_mixed_kernel(ewt_tree& t, uint8_t const* types, void const* in,
   PhaseTimer pt(EWT_PHASE_QUERY, s);
   mk<<<blocks, threads, p.bytes, s>>>(t.view, types,
                                       static_cast<QueryRec<T> const*>(in), m,
-                                      out, err, p.stage_counts, p.stage_ranks);
+                                      out, err, p.stage_counts, p.stage_ranks,
+                                      queue);
   EWT_LAUNCHED();
 }
 
@@ -323,7 +328,7 @@ void launch_typed(ewt_tree& t, uint8_t const* types, void const* in,
   RelaxedCapture relaxed;  // these launches may be captured into a graph
   if (K == kMixed) {
     launch_mixed_kernel<T>(t, types, in, m, static_cast<uint64_t*>(out),
-                           t.err_d.as<uint32_t>(), p, s);
+                           t.err_d.as<uint32_t>(), p, s, queue_slot(t));
     return;
   }
   auto k = query_kernel<T, K>;
@@ -385,7 +390,8 @@ template <class T>
 void launch_mixed_raw_typed(ewt_tree& t, uint8_t const* d_types,
                             void const* d_q, uint64_t m, uint64_t* d_out,
                             uint32_t* d_err, cudaStream_t s) {
-  launch_mixed_kernel<T>(t, d_types, d_q, m, d_out, d_err, plan_stage(t), s);
+  launch_mixed_kernel<T>(t, d_types, d_q, m, d_out, d_err, plan_stage(t), s,
+                         work_queue_enabled() ? d_err + 16 : nullptr);
 }
 }  // namespace
 

@@ -525,4 +525,18 @@ void build_dense_samples(RSStore& rs, uint32_t shift, cudaStream_t stream) {
   EWT_CUDA(cudaStreamSynchronize(stream));
 }
 
+uint64_t rs_bytes_bound(uint64_t bits, uint32_t arrays, bool with_support) {
+  uint64_t const words = (ceil_div(ceil_div(bits, 32), 32) * 32 + 2) * 4;
+  uint64_t const l1 = (ceil_div(bits, kL1Bits) + 1) * 8;
+  uint64_t const l2 = (ceil_div(bits, kL2Bits) + 1) * 2;
+  uint64_t per = words + l1 + l2 + sizeof(ArrayMeta) + 64;
+  if (with_support) {
+    uint64_t const samples = (bits / kSampleRate + 2) * 8;
+    uint64_t const blocks = (ceil_div(bits, 224) + 1) * 32 + 8;
+    uint64_t const dense = (bits / 32 + 2) * 4;  // densest rate (32)
+    per += samples + blocks + dense;
+  }
+  return per * arrays + 64;
+}
+
 }  // namespace ewt

@@ -677,8 +677,8 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   auto const level_nodes = make_level_nodes(sigma, L);
 
   // ---- device tables
-  t.err_d.alloc(16);
-  EWT_CUDA(cudaMemsetAsync(t.err_d.get(), 0, 16, st));
+  t.err_d.alloc(kTreeErrBytes);
+  EWT_CUDA(cudaMemsetAsync(t.err_d.get(), 0, kTreeErrBytes, st));
   uint32_t* err_build = t.err_d.as<uint32_t>() + 1;
   uint32_t const grid_stream =
       static_cast<uint32_t>(std::min<uint64_t>(ceil_div(n, 256),
@@ -922,6 +922,34 @@ void build_tree(ewt_tree& t, const void* data, uint64_t n, int elem_size,
     default:
       throw Error(EWT_ERR_INVALID_ARGUMENT, "elem_size must be 1, 2, 4 or 8");
   }
+}
+
+void minimal_codes(uint64_t sigma, std::vector<uint64_t>& lens,
+                   std::vector<uint64_t>& codes) {
+  lens.clear();
+  codes.clear();
+  for (CodeH const& c : make_codes(sigma)) {
+    lens.push_back(c.len);
+    codes.push_back(c.code);
+  }
+}
+
+uint64_t build_bytes_bound(uint64_t n, uint32_t elem_size, uint64_t sigma) {
+  uint64_t const L = sigma < 2 ? 1 : h_ceil_log2(sigma);
+  uint64_t const text = n * elem_size;
+  // resident: level bits, L1/L2/samples, and the query side (group levels
+  // or rank blocks, and dense select samples: below 2.5 times the level
+  // bits -- octal blocks add 61 % and their samples 33 %)
+  uint64_t const level_bits = L * (ceil_div(n, 32) + 64) * 4;
+  uint64_t const support = L * (n / 8192 * 8 + n / 256 + n / 512 + 256);
+  uint64_t const query = 5 * level_bits / 2;
+  // count table, node ranks and node bases (per symbol and level)
+  uint64_t const shape = (sigma + 1) * 8 * 4 + L * 64;
+  // transient: a copy of a host text, two level orders of the widest
+  // minimal symbol, chunk tables and scratch
+  uint64_t const order = n * std::max<uint32_t>(elem_size, L > 16 ? 4 : (L > 8 ? 2 : 1));
+  uint64_t const transient = text + 2 * order + n / 64 + (64ull << 20);
+  return level_bits + support + query + shape + transient;
 }
 
 }  // namespace ewt

@@ -48,6 +48,28 @@ class RankSelect {
   __host__ RankSelect(detail::RSView const& v, uint64_t const* host_bits)
       : bit_array_(v, host_bits), is_copy_(true) {}
 
+  /* Standalone, from bit arrays the caller created with BitArray(sizes[,
+   * init_value]) and filled on the device: takes them over and builds the
+   * counts and samples in place (all device work is waited for first).
+   * Throws std::runtime_error on failure (the reference's constructor is
+   * noexcept and aborts). */
+  __host__ RankSelect(BitArray&& bit_array, uint32_t const GPU_index)
+      : is_copy_(false) {
+    (void)GPU_index;  // the arrays stay on the GPU they were created on
+    if (!bit_array.owns_ || !bit_array.handle_)
+      throw std::runtime_error(
+          "RankSelect(BitArray&&) needs a BitArray that owns its arrays");
+    host_bits_ = std::move(bit_array.own_bits_);
+    handle_ = bit_array.handle_;
+    bit_array.handle_ = nullptr;
+    bit_array.owns_ = false;
+    int const st = ewt_rs_build_in_place(handle_);
+    if (st != EWT_OK) throw std::runtime_error(ewt_last_error());
+    detail::RSView v;
+    ewt_rs_get_device_view(handle_, &v, sizeof(v));
+    bit_array_ = BitArray(v, host_bits_.data());
+  }
+
   /* Standalone: bit arrays given as packed words (host or device memory),
    * one array after the other, ceil(bits[a]/32) words each. */
   __host__ RankSelect(uint32_t const* words, std::vector<size_t> const& bits,
@@ -69,7 +91,7 @@ class RankSelect {
   __host__ RankSelect& operator=(RankSelect&& o) noexcept {
     if (this != &o) {
       release();
-      bit_array_ = o.bit_array_;
+      bit_array_ = BitArray(o.bit_array_);  // a non-owning copy
       handle_ = o.handle_;
       host_bits_ = std::move(o.host_bits_);
       is_copy_ = o.is_copy_;
@@ -130,6 +152,15 @@ class RankSelect {
     return Value ? v.s1[v.meta[a].s1_off + index]
                  : v.s0[v.meta[a].s0_off + index];
   }
+  /* Upper bound of the device bytes of num_arrays arrays of size bits with
+   * their rank/select support. */
+  __host__ static size_t getNeededGPUMemory(size_t const size,
+                                            uint8_t const num_arrays) {
+    uint64_t b = 0;
+    ewt_needed_memory(EWT_MEM_RANKSELECT, size, num_arrays, 0, &b);
+    return b;
+  }
+
   __device__ RSConfig::L1_TYPE getL1Entry(uint32_t a, size_t index) const {
     detail::RSView const& v = bit_array_.view();
     return v.l1[v.meta[a].l1_off + index];

@@ -182,6 +182,12 @@ class WaveletTree {
   __device__ size_t getPrecomputedRank(T const i) const {
     return view_.node_ranks[i];
   }
+  /* Overwrites node rank i, the value getPrecomputedRank(i) returns and the
+   * walks over binary levels read (walks over group levels use their own
+   * per-node digit counts). */
+  __device__ void setPrecomputedRank(T const i, size_t const rank) {
+    const_cast<uint64_t*>(view_.node_ranks)[i] = rank;
+  }
   __device__ T getNumNodesAtLevel(uint8_t const level) const {
     return static_cast<T>(view_.nodes_at_level[level]);
   }
@@ -189,43 +195,33 @@ class WaveletTree {
   __host__ ewt_tree* handle() const { return handle_; }
 
   /* Shortened codes of the last symbols when the alphabet size is not a
-   * power of two (createMinimalCodes). */
+   * power of two (createMinimalCodes): the library's own codes, the ones
+   * its builds use. */
   __host__ static std::vector<Code> createMinimalCodes(
       std::vector<T> const& alphabet) {
     uint64_t const sigma = alphabet.size();
-    if (utils::isPowTwo<uint64_t>(sigma)) return {};
-    uint32_t const bits = utils::ceilLog2<uint64_t>(sigma);
-    std::vector<uint64_t> len(sigma, bits), code(sigma);
-    for (uint64_t i = 0; i < sigma; ++i) code[i] = i;
-    uint32_t start_bit = 0, code_len = bits;
-    uint64_t start_i = 0, left = sigma, kept = 0;
-    do {
-      for (uint32_t i = code_len - 1; i > 0; --i) {
-        uint64_t const p = uint64_t(1) << i;
-        if (left <= p) break;
-        left -= p;
-        start_i += p;
-        ++start_bit;
-      }
-      if (code_len == bits) kept = left;
-      if (left == 1) {
-        code_len = 1;
-        len[sigma - 1] = start_bit;
-        code[sigma - 1] = ((uint64_t(1) << start_bit) - 1) << (bits - start_bit);
-      } else {
-        code_len = utils::ceilLog2<uint64_t>(left);
-        uint64_t const high = ~((uint64_t(1) << (bits - start_bit)) - 1);
-        for (uint64_t i = sigma - left; i < sigma; ++i) {
-          code[i] = ((i - start_i) << (bits - start_bit - code_len)) +
-                    (high & code[i]);
-          len[i] = start_bit + code_len;
-        }
-      }
-    } while (code_len > 1);
-    std::vector<Code> out;
-    for (uint64_t i = sigma - kept; i < sigma; ++i)
-      out.push_back(Code{static_cast<uint8_t>(len[i]), static_cast<T>(code[i])});
+    if (sigma < 2 || utils::isPowTwo<uint64_t>(sigma)) return {};
+    uint64_t count = 0;
+    if (ewt_minimal_codes(sigma, nullptr, nullptr, 0, &count) != EWT_OK)
+      throw std::runtime_error(ewt_last_error());
+    std::vector<uint64_t> len(count), code(count);
+    ewt_minimal_codes(sigma, len.data(), code.data(), count, &count);
+    std::vector<Code> out(count);
+    for (uint64_t i = 0; i < count; ++i)
+      out[i] = Code{static_cast<uint8_t>(len[i]), static_cast<T>(code[i])};
     return out;
+  }
+
+  /* Upper bound of the device bytes a build of data_size symbols over
+   * alphabet_size symbols holds at its peak (the finished tree included);
+   * num_levels and num_codes follow from the alphabet size here. */
+  __host__ static size_t getNeededGPUMemory(size_t const data_size,
+                                            size_t const alphabet_size,
+                                            uint8_t const /*num_levels*/,
+                                            T const /*num_codes*/) {
+    uint64_t b = 0;
+    ewt_needed_memory(EWT_MEM_TREE, data_size, sizeof(T), alphabet_size, &b);
+    return b;
   }
 
  private:

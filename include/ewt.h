@@ -189,6 +189,47 @@ int ewt_rs_select(ewt_rs* rs, int array, int value, const uint64_t* i,
 int ewt_rs_get_device_view(const ewt_rs* rs, void* view_out,
                            uint64_t view_size);
 
+/* Bit arrays that the caller fills on the device, then gives rank/select
+ * support.  ewt_bitarray_create lays out num_arrays arrays of bits[a] bits
+ * (1 to 255 arrays, the ewt_rs_build layout: each array padded to 32
+ * words) with every bit set to init_value (0 or 1); the caller's kernels
+ * write them through the device view (ewt_rs_get_device_view: RSView::words
+ * at ArrayMeta::word_off); rank and select are refused until
+ * ewt_rs_build_in_place.  Replaces BitArray(sizes) and BitArray(sizes,
+ * init_value) (bit_array.cuh:61,70; bit_array.cu:40-100; the reference leaves
+ * the words of the first form uninitialised, here they are zero). */
+int ewt_bitarray_create(const uint64_t* bits, uint32_t num_arrays,
+                        int init_value, int gpu_index, ewt_rs** out);
+/* Builds the L1/L2 counts, select samples and query-side blocks over the
+ * words the caller wrote, in place (bits past an array's end are cleared);
+ * first waits for all work on the device, since the kernels that wrote the
+ * words may run on any stream.  Replaces RankSelect(BitArray&&, GPU_index)
+ * (rank_select.cuh:94; rank_select.cu:50-304). */
+int ewt_rs_build_in_place(ewt_rs* rs);
+
+/* Upper bound of the device bytes of: EWT_MEM_BITARRAY, num_arrays bit
+ * arrays of n bits each (ewt_bitarray_create); EWT_MEM_RANKSELECT, the same
+ * with their rank/select support (ewt_rs_build, ewt_rs_build_in_place);
+ * EWT_MEM_TREE, a build of n elem_size-byte symbols over sigma symbols at its
+ * peak (the finished tree, a device copy of a host text and the build's
+ * transient level orders).  Replaces BitArray::getNeededGPUMemory
+ * (bit_array.cuh:332), RankSelect::getNeededGPUMemory (rank_select.cuh:818)
+ * and WaveletTree::getNeededGPUMemory (wavelet_tree.cuh:2544), whose figures
+ * describe the reference's own allocations. */
+#define EWT_MEM_BITARRAY 0
+#define EWT_MEM_RANKSELECT 1
+#define EWT_MEM_TREE 2
+int ewt_needed_memory(int kind, uint64_t n, uint32_t num_arrays_or_elem_size,
+                      uint64_t sigma, uint64_t* bytes);
+
+/* The shortened codes (length, code; code aligned to the top of
+ * ceil(log2 sigma) bits) of the last *count symbols of 0..sigma-1 when
+ * sigma is not a power of two, none otherwise; at most cap are written.
+ * The codes the builds use.  Replaces WaveletTree::createMinimalCodes
+ * (wavelet_tree.cuh:2100-2159). */
+int ewt_minimal_codes(uint64_t sigma, uint64_t* lens, uint64_t* codes,
+                      uint64_t cap, uint64_t* count);
+
 /* ---- diagnostics ------------------------------------------------------- */
 /* Per-phase device time, measured with CUDA events recorded on the stream
  * each kernel is launched on.  Off by default; enabling adds a stream
@@ -216,6 +257,14 @@ const char* ewt_last_error(void); /* message of the calling thread's last
 int ewt_abi_version(void);
 /* Number of kernel launches this library issued since load (all threads). */
 uint64_t ewt_launch_count(void);
+/* Batched query launches (ewt_mixed*, ewt_mixed_multi*) hand their chunks
+ * to CTAs from a device work queue, an atomic chunk counter, by default;
+ * enable = 0 switches to a fixed stride (CTA b takes chunks b, b + G, ...)
+ * for comparisons.  Results never depend on it.  Launches already captured
+ * in a graph keep the form they were captured with.  No reference
+ * counterpart (the reference strides by the grid size, wavelet_tree.cuh:
+ * 373-544). */
+void ewt_set_work_queue(int enable);
 /* SM version (major * 10 + minor, e.g. 103) of the library code that runs
  * on GPU gpu_index, as the CUDA runtime reports it for the query kernel.
  * No reference counterpart (diagnostic). */

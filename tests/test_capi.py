@@ -62,3 +62,37 @@ def test_errors_without_gpu_are_statuses(ewt):
     st = lib.ewt_build(np.zeros(4, np.uint8).ctypes.data, 4, 3, None, 0, 0,
                        ctypes.byref(h))
     assert st == -1
+
+
+def test_minimal_codes_entry_matches_oracle(ewt, oracle):
+    """ewt_minimal_codes (what WaveletTree::createMinimalCodes returns) gives
+    the codes of the oracle's restatement, which the known answers pin."""
+    lib = ctypes.CDLL(ewt.LIB_PATH)
+    import numpy as np
+    for sigma in (3, 5, 10, 63, 72, 75, 255, 1000, 65535, 256):
+        cnt = ctypes.c_uint64()
+        assert lib.ewt_minimal_codes(ctypes.c_uint64(sigma), None, None,
+                                     ctypes.c_uint64(0), ctypes.byref(cnt)) == 0
+        lens = np.zeros(cnt.value, np.uint64)
+        codes = np.zeros(cnt.value, np.uint64)
+        assert lib.ewt_minimal_codes(ctypes.c_uint64(sigma),
+                                     lens.ctypes.data_as(ctypes.c_void_p),
+                                     codes.ctypes.data_as(ctypes.c_void_p),
+                                     ctypes.c_uint64(cnt.value),
+                                     ctypes.byref(cnt)) == 0
+        got = [(int(l), int(c)) for l, c in zip(lens, codes)]
+        assert got == oracle.minimal_codes(sigma), sigma
+
+
+def test_needed_memory_entry(ewt):
+    lib = ewt.lib()
+    b = ctypes.c_uint64()
+    assert lib.ewt_needed_memory(0, 1 << 20, 3, 0, ctypes.byref(b)) == 0
+    ba = b.value
+    assert ba >= 3 * (1 << 20) // 8
+    assert lib.ewt_needed_memory(1, 1 << 20, 3, 0, ctypes.byref(b)) == 0
+    assert b.value > ba
+    assert lib.ewt_needed_memory(2, 1 << 30, 1, 256, ctypes.byref(b)) == 0
+    assert b.value > (1 << 30)
+    assert lib.ewt_needed_memory(2, 1 << 30, 3, 256, ctypes.byref(b)) == -1
+    assert lib.ewt_needed_memory(7, 1, 1, 1, ctypes.byref(b)) == -1

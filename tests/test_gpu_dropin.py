@@ -49,3 +49,68 @@ def test_dropin_example(ewt, oracle, tmp_path, n, sigma):
     bits = np.unpackbits(lvl0.view(np.uint8), bitorder="little")
     csum = np.concatenate([[0], np.cumsum(bits, dtype=np.uint64)])
     assert np.array_equal(dev[:, 3], csum[idx.astype(np.int64)])
+
+
+@pytest.mark.parametrize("init", [0, 1])
+def test_bitarray_filled_by_user_kernel(ewt, oracle, tmp_path, init):
+    """BitArray(sizes[, init]) filled by a user kernel (writeWord /
+    writeWordAtBit), moved into RankSelect(BitArray&&, gpu), queried by a
+    user kernel: every rank (both values, with the bit) and select answer,
+    and the total ones, equal the oracle's restatement of the reference's
+    RankSelect over the same words."""
+    from ecl_wavelet_gb300 import dropin
+    exe = dropin.build_example("bitarray_example")
+    out = tmp_path / "ba.bin"
+    r = subprocess.run([exe, str(init), "4242", str(out)], capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    raw = out.read_bytes()
+    A, m, init_, need_ba, need_rs = (int(v) for v in np.frombuffer(raw[:40], np.uint64))
+    assert init_ == init
+    off = 40
+    sizes = np.frombuffer(raw[off:off + 8 * A], np.uint64).astype(np.int64)
+    off += 8 * A
+    assert need_rs > need_ba >= int(sizes.sum()) // 8
+    words, queries = [], []
+    for a in range(A):
+        nw = (int(sizes[a]) + 31) // 32
+        words.append(np.frombuffer(raw[off:off + 4 * nw], np.uint32))
+        off += 4 * nw
+        pos = np.frombuffer(raw[off:off + 8 * m], np.uint64); off += 8 * m
+        k1 = np.frombuffer(raw[off:off + 8 * m], np.uint64); off += 8 * m
+        k0 = np.frombuffer(raw[off:off + 8 * m], np.uint64); off += 8 * m
+        res = np.frombuffer(raw[off:off + 48 * m], np.uint64).reshape(m, 6)
+        off += 48 * m
+        queries.append((pos, k1, k0, res))
+    ors = oracle.OracleRS(words, sizes)
+    ones = ors.export("TOTAL_ONES")
+    for a, (pos, k1, k0, res) in enumerate(queries):
+        r1 = ors.rank_batch(a, pos, 1)
+        assert np.array_equal(res[:, 0], r1), a
+        assert np.array_equal(res[:, 1], pos - r1), a
+        w = words[a]
+        p = pos.astype(np.int64)
+        inside = p < int(sizes[a])
+        bit = np.zeros(m, np.uint64)
+        bit[inside] = (w[p[inside] // 32] >> (p[inside] % 32).astype(np.uint32)) & 1
+        assert np.array_equal(res[:, 2], bit), a
+        assert np.array_equal(res[:, 3], ors.select_batch(a, k1, 1)), a
+        assert np.array_equal(res[:, 4], ors.select_batch(a, k0, 0)), a
+        assert np.all(res[:, 5] == ones[a]), a
+
+
+def test_needed_memory_bounds_built_trees(ewt):
+    """WaveletTree::getNeededGPUMemory's figure (ewt_needed_memory) bounds the
+    device bytes of the finished trees it describes."""
+    import ctypes
+    rng = np.random.default_rng(8)
+    for dtype, sigma, n in ((np.uint8, 256, 3_000_000), (np.uint8, 5, 2_000_000),
+                            (np.uint16, 1000, 1_000_000),
+                            (np.uint32, 70_000, 500_000)):
+        text = rng.integers(0, sigma, n).astype(dtype)
+        t = ewt.WaveletTree(text, np.arange(sigma))
+        b = ctypes.c_uint64()
+        assert ewt.lib().ewt_needed_memory(2, n, np.dtype(dtype).itemsize,
+                                           sigma, ctypes.byref(b)) == 0
+        assert t.info.device_bytes <= b.value, (dtype, sigma)
+        t.close()
