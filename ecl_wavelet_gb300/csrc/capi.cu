@@ -35,6 +35,13 @@ cudaMemPool_t lib_pool() {
     EWT_CUDA(cudaMemPoolCreate(&pools[dev], &props));
     uint64_t keep = UINT64_MAX;
     EWT_CUDA(cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep));
+    // A block freed on one stream is handed to another stream only once the
+    // free has completed, never with an inserted wait on the first stream:
+    // builds and query batches on different streams (a batch build runs
+    // one stream per text) must not serialise through reused blocks.
+    int no = 0;
+    EWT_CUDA(cudaMemPoolSetAttribute(
+        pools[dev], cudaMemPoolReuseAllowInternalDependencies, &no));
   }
   return pools[dev];
 }

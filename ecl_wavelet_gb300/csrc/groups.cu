@@ -1117,6 +1117,46 @@ bool octal_text_eligible(ewt_tree const& t, uint32_t elem_size) {
   return groups_eligible(t) && elem_size <= 2 && group_widths(t.L).front() == 3;
 }
 
+// The routing and digit tables in device memory, uploaded once per device
+// (every later build on it reads the same copy; held until exit).
+template <class V>
+V const* lut_on_device(std::vector<V> const& host, V* (&cache)[64]) {
+  static std::mutex mu;
+  int dev = 0;
+  EWT_CUDA(cudaGetDevice(&dev));
+  EWT_REQUIRE(dev >= 0 && dev < 64, EWT_ERR_INVALID_ARGUMENT,
+              "device index out of range");
+  std::lock_guard<std::mutex> lk(mu);
+  if (!cache[dev]) {
+    V* p = nullptr;
+    EWT_CUDA(cudaMalloc(&p, host.size() * sizeof(V)));
+    EWT_CUDA(cudaMemcpy(p, host.data(), host.size() * sizeof(V),
+                        cudaMemcpyHostToDevice));
+    cache[dev] = p;
+  }
+  return cache[dev];
+}
+
+uint8_t const* route_lut_on_device() {
+  static std::vector<uint8_t> const lut8 = [] {
+    std::vector<uint8_t> v;
+    make_route_lut(v);
+    return v;
+  }();
+  static uint8_t* cache[64] = {};
+  return lut_on_device(lut8, cache);
+}
+
+uint16_t const* digit_lut_on_device() {
+  static std::vector<uint16_t> const lut = [] {
+    std::vector<uint16_t> v;
+    make_digit_lut(v);
+    return v;
+  }();
+  static uint16_t* cache[64] = {};
+  return lut_on_device(lut, cache);
+}
+
 void build_octal_level0(ewt_tree& t, void const* sym, uint32_t elem_size,
                         uint32_t* level0, bool check, uint32_t* err, cudaStream_t st) {
   t.groups.level0_built = false;
@@ -1174,32 +1214,20 @@ void build_groups(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
                            cudaMemcpyHostToDevice, st));
   layout_group_samples(qs, qs.sel_shift);
   upload_levels(qs, st);
-  static std::vector<uint16_t> const lut = [] {
-    std::vector<uint16_t> v;
-    make_digit_lut(v);
-    return v;
-  }();
-  static std::vector<uint8_t> const lut8 = [] {
-    std::vector<uint8_t> v;
-    make_route_lut(v);
-    return v;
-  }();
-  DevBuf lut_d, lut8_d, plane, err_d(4);
+  DevBuf plane, err_d(4);
   EWT_CUDA(cudaMemsetAsync(err_d.get(), 0, 4, st));
   uint64_t plane_words = 0;
+  uint8_t const* lut8_d = nullptr;
+  uint16_t const* lut_d = nullptr;
   if (any_octal) {
-    lut8_d.alloc(lut8.size());
-    EWT_CUDA(cudaMemcpyAsync(lut8_d.get(), lut8.data(), lut8.size(),
-                             cudaMemcpyHostToDevice, st));
+    lut8_d = route_lut_on_device();
     plane_words = ceil_div(n, 64) * 2 + 16;  // slack for the 64-bit reads
     plane.alloc(plane_words * 4);
     set_smem_limit(merge_plane_kernel, 65536);
     set_smem_limit(octal_level_kernel, 65536);
   }
   if (widths.back() == 2) {
-    lut_d.alloc(lut.size() * 2);
-    EWT_CUDA(cudaMemcpyAsync(lut_d.get(), lut.data(), lut.size() * 2,
-                             cudaMemcpyHostToDevice, st));
+    lut_d = digit_lut_on_device();
     set_smem_limit(quad_level_kernel, 65536 * 2);
   }
   DevBuf chunk(ceil_div(max_info + 1, kScanChunk) * 8 * 8);
@@ -1224,7 +1252,7 @@ void build_groups(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
           static_cast<uint32_t>(std::min<uint64_t>(ceil_div(nsb, 2), uint64_t(sms)));
       quad_level_kernel<<<grid, 1024, 65536 * 2, st>>>(
           v, lv, ql, words + m0.word_off, ceil_div(n, 32), words + m1.word_off,
-          total_words - m1.word_off, lut_d.as<uint16_t>(), blocks, sb,
+          total_words - m1.word_off, lut_d, blocks, sb,
           info.as<SbStart>(), nsb, qs.ds.get() ? qs.ds.as<uint32_t>() : nullptr,
           err_d.as<uint32_t>());
       EWT_LAUNCHED();
@@ -1248,7 +1276,7 @@ void build_groups(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
                              std::min<uint64_t>(ceil_div(nsb_m, 2), uint64_t(sms))),
                          1024, 65536, st>>>(
         v, lv + 1, words + m1.word_off, words + m2.word_off, total_words - m2.word_off,
-        lut8_d.as<uint8_t>(), info.as<SbStart>(), nsb_m, plane.as<uint32_t>(),
+        lut8_d, info.as<SbStart>(), nsb_m, plane.as<uint32_t>(),
         err_d.as<uint32_t>());
     EWT_LAUNCHED();
     sb_info_kernel<<<static_cast<uint32_t>(ceil_div(nsb, 128)), 128, 0, st>>>(
@@ -1257,7 +1285,7 @@ void build_groups(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
     EWT_CUDA(cudaMemsetAsync(sb + nsb * 8, 0, 64, st));  // the totals entry
     octal_level_kernel<<<grid_o, 1024, 65536, st>>>(
         v, lv, words + m0.word_off, words + m1.word_off, total_words - m1.word_off,
-        plane.as<uint32_t>(), plane_words, lut8_d.as<uint8_t>(), info.as<SbStart>(), nsb,
+        plane.as<uint32_t>(), plane_words, lut8_d, info.as<SbStart>(), nsb,
         ql.num_blocks, blocks, sb, err_d.as<uint32_t>());
     EWT_LAUNCHED();
     scan_superblocks<8>(sb, nsb + 1, chunk, st);

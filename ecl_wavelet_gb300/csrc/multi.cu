@@ -49,7 +49,7 @@ constexpr uint32_t kMultiChunk = 2048;
 constexpr uint32_t kMultiThreads = 256;
 constexpr uint32_t kPlanThreads = 1024;
 constexpr uint32_t kMaxMultiTrees = 1u << 16;  // trees in one call
-constexpr uint32_t kBuildWorkers = 8;           // host threads of a batch build
+constexpr uint32_t kBuildWorkers = 16;          // host threads of a batch build
 
 __global__ void __launch_bounds__(256)
 tree_hist_kernel(uint32_t const* __restrict__ tree_of, uint64_t m,

@@ -456,7 +456,17 @@ void run_passes(ewt_tree& t, T const* sym, uint64_t n, uint32_t* err,
   uint32_t* const words = t.rs.words.as<uint32_t>();
   uint64_t const w1 = t.rs.meta[1].word_off;
   EWT_CUDA(cudaMemsetAsync(words + w1, 0, (t.rs.total_words - w1) * 4, st));
-  uint64_t const max_chunks = n / kPChunk + (uint64_t(1) << kPMaxStartLevel) + 2;
+  // chunks of a pass starting at level a: at most n / kPChunk + 2^a (one
+  // partial chunk per level-a node); tables sized for the deepest start
+  uint32_t a_last = 0;
+  for (uint32_t i = 0, a = 0; i < np; ++i) {
+    a_last = a;
+    a += levels / np + (i < levels % np ? 1u : 0u);
+  }
+  auto chunks_at = [&](uint32_t a) {
+    return n / kPChunk + (uint64_t(1) << a) + 2;
+  };
+  uint64_t const max_chunks = chunks_at(a_last);
   DevBuf chunk_first(((uint64_t(1) << kPMaxStartLevel) + 1) * 4);
   DevBuf chunk_tot(max_chunks * kPMaxDigits * 4);
   DevBuf chunk_pre(max_chunks * kPMaxDigits * 8);
@@ -494,8 +504,11 @@ void run_passes(ewt_tree& t, T const* sym, uint64_t n, uint32_t* err,
       if (!ob.get()) ob.alloc(n * sizeof(T) + 64);
       next = ob.as<T>();
     }
+    // grids follow the pass's chunk count, so a small text's launches leave
+    // the GPU to other streams' work
+    uint64_t const pass_chunks = chunks_at(a);
     uint32_t const grid = static_cast<uint32_t>(
-        std::min<uint64_t>(max_chunks, uint64_t(sms) * 5));
+        std::min<uint64_t>(pass_chunks, uint64_t(sms) * 5));
     {
       PhaseTimer pt(EWT_PHASE_HIST, st);
       chunk_table_kernel<<<1, 1024, 0, st>>>(pa);
@@ -505,13 +518,13 @@ void run_passes(ewt_tree& t, T const* sym, uint64_t n, uint32_t* err,
         // for a host text, its copy to the device)
         PhaseTimer pt2(ingest_copy ? EWT_PHASE_H2D : EWT_PHASE_FILL, st);
         ingest_kernel<T><<<static_cast<uint32_t>(std::min<uint64_t>(
-                               max_chunks, uint64_t(sms) * 6)),
+                               pass_chunks, uint64_t(sms) * 6)),
                            kPThreads, 0, st>>>(ingest_src,
                                                ingest_copy ? const_cast<T*>(cur) : nullptr,
                                                words + t.rs.meta[0].word_off, pa);
       } else {
         digit_count_kernel<T><<<static_cast<uint32_t>(std::min<uint64_t>(
-                                    max_chunks, uint64_t(sms) * 6)),
+                                    pass_chunks, uint64_t(sms) * 6)),
                                 kPThreads, 0, st>>>(cur, pa);
       }
       EWT_LAUNCHED();
