@@ -187,6 +187,10 @@ void build_tree(ewt_tree& t, const void* data, uint64_t n, int elem_size,
 // synchronises once before it starts; wt_build.cu).
 void set_texts_synchronized(bool v);
 bool texts_synchronized();
+// Builds on this thread belong to a batch (ewt_build_batch): texts shorter
+// than kBatchGroupMinSymbols get rank blocks instead of group query levels.
+constexpr uint64_t kBatchGroupMinSymbols = uint64_t(1) << 22;
+void set_batch_member(bool v);
 // Sets t.view from the tree's device buffers and shape (wt_build.cu).
 void fill_tree_view(ewt_tree& t);
 // Shortened codes (length, code) of the last symbols of a non-power-of-two

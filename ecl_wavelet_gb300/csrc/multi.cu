@@ -686,6 +686,7 @@ extern "C" int ewt_build_batch(const void* const* texts, const uint64_t* lengths
     }
     auto work = [&] {
       set_texts_synchronized(true);
+      set_batch_member(true);
       for (uint32_t i = next++; i < count; i = next++) {
         int const st = ewt_build(texts[i], lengths[i], elem_size,
                                  alphabets ? alphabets[i] : nullptr,
@@ -700,6 +701,7 @@ extern "C" int ewt_build_batch(const void* const* texts, const uint64_t* lengths
         }
       }
       set_texts_synchronized(false);
+      set_batch_member(false);
     };
     std::vector<std::thread> pool;
     for (uint32_t w = 1; w < workers; ++w) pool.emplace_back(work);

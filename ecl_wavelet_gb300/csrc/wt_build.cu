@@ -547,6 +547,7 @@ void run_passes(ewt_tree& t, T const* sym, uint64_t n, uint32_t* err,
 }
 
 thread_local bool t_texts_synced = false;
+thread_local bool t_batch_member = false;
 
 // Whether a host text goes straight to the first pass's ingest kernel
 // (kernels read the host text: a Grace host's pageable memory, or pinned
@@ -788,7 +789,13 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   // ---- level 0 bits (with an ingested host text: written by the first pass)
   uint32_t* const words = t.rs.words.as<uint32_t>();
   t.groups.level0_built = false;
-  if (!ingest && t.pow2 && octal_text_eligible(t, sizeof(T))) {
+  // Group query levels for power-of-two alphabets -- except for the small
+  // texts of a batch build: their trees stay in L2 when queried (so group
+  // levels save little) while the group build's launch latency would be
+  // most of their build time; they get rank blocks on every level instead.
+  bool const want_groups =
+      groups_eligible(t) && !(t_batch_member && n < kBatchGroupMinSymbols);
+  if (!ingest && want_groups && octal_text_eligible(t, sizeof(T))) {
     // level 0 is the octal level 0's top bit plane: both in one read
     build_octal_level0(t, sym, sizeof(T), words + t.rs.meta[0].word_off, t.is_min,
                        err_build, st);
@@ -868,7 +875,7 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   build_rs_samples(t.rs, st);
   // binary levels that group levels cover get no rank blocks
   t.rs.skip_blocks.assign(L, 0);
-  if (groups_eligible(t)) {
+  if (want_groups) {
     uint32_t covered = 0;
     for (uint32_t w : group_widths(L)) covered += w;
     for (uint32_t l = 0; l < covered; ++l) t.rs.skip_blocks[l] = 1;
@@ -891,7 +898,7 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   t.counts.assign(c.begin(), c.begin() + sigma);
   t.occ.resize(sigma);
   for (uint64_t i = 0; i < sigma; ++i) t.occ[i] = c[i + 1] - c[i];
-  build_groups(t, c, sym, sizeof(T), st);
+  if (want_groups) build_groups(t, c, sym, sizeof(T), st);
   v.groups = t.groups.view();
 }
 
@@ -899,6 +906,7 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
 
 void set_texts_synchronized(bool v) { t_texts_synced = v; }
 bool texts_synchronized() { return t_texts_synced; }
+void set_batch_member(bool v) { t_batch_member = v; }
 
 void fill_tree_view(ewt_tree& t) {
   TreeView& v = t.view;

@@ -324,9 +324,13 @@ int ewt_load(const char* path, int gpu_index, ewt_tree** out);
  * Builds `count` texts (elem_size bytes per symbol) concurrently, each on its
  * own stream: out[i] receives tree i (NULL when its build failed, with
  * statuses[i], if given, holding its status).  alphabets / sigmas may be
- * NULL (every alphabet detected).  Returns the first failing status.  The
- * reference builds one tree per constructor call (wavelet_tree.cuh:576-867);
- * no reference counterpart for the batch. */
+ * NULL (every alphabet detected).  Returns the first failing status.
+ * Answers never differ from single builds'; the query-side structures may:
+ * texts shorter than 2^22 symbols get rank blocks on every level instead of
+ * group query levels (their trees are small enough to stay in L2 when
+ * queried, and the group build's launches would dominate their build time).
+ * The reference builds one tree per constructor call (wavelet_tree.cuh:
+ * 576-867); no reference counterpart for the batch. */
 int ewt_build_batch(const void* const* texts, const uint64_t* lengths,
                     uint32_t count, int elem_size,
                     const void* const* alphabets, const uint64_t* sigmas,
