@@ -469,6 +469,7 @@ pass_kernel(T const* __restrict__ src, T* __restrict__ dst, PassArgs p) {
   __shared__ uint64_t gpos[kPMaxDigits];             // level-b run starts
   __shared__ uint64_t rgw[kPMaxK + 1][kPMaxDigits];  // first word of a bit run
   __shared__ uint32_t rgs[kPMaxK + 1][kPMaxDigits];  // its first bit there
+  __shared__ uint16_t wpre[kPMaxK + 1][kPMaxDigits + 1];  // words before a run
   __shared__ ChunkInfo ck;
   __shared__ uint32_t fix_n[2];  // threads whose symbols span a class boundary
   __shared__ uint16_t fix_list[kPThreads];
@@ -635,18 +636,23 @@ pass_kernel(T const* __restrict__ src, T* __restrict__ dst, PassArgs p) {
           fence_async_shared();
           if (pc < total_chunks) issue(stage);
         }
-        // -- b. level a+r bits out (level a's came from the previous pass);
-        //    warp w writes runs w, w + 8, ... one output word per lane.
+        // -- b. level a+r bits out (level a's came from the previous pass):
+        //    the output words of all class runs, numbered run after run
+        //    (wpre), spread over every thread of the CTA.
         if (r >= 1) {
           uint32_t const runs = 1u << r;
           uint32_t const* bb = bitbuf[r & 1];
           uint32_t* const out = p.words + p.word_off[r];
-          for (uint32_t cc = wid; cc < runs; cc += kPWarps) {
+          uint32_t const total_w = wpre[r][runs];
+          for (uint32_t f = tid; f < total_w; f += kPThreads) {
+            uint32_t cc = 0;  // the run holding output word f
+            for (uint32_t st = runs >> 1; st; st >>= 1)
+              if (wpre[r][cc + st] <= f) cc += st;
+            uint32_t const du = f - wpre[r][cc];
             uint32_t const cs = cls[r][cc], len = cls[r][cc + 1] - cs;
             uint32_t const gsh = rgs[r][cc];
             uint64_t const gwb = rgw[r][cc];
-            uint32_t const nw = len ? (gsh + len + 31) >> 5 : 0u;
-            for (uint32_t du = lane; du < nw; du += 32) {
+            {
               uint32_t const raw = bits_from(
                   bb, static_cast<int32_t>(cs + 32 * du) - static_cast<int32_t>(gsh));
               uint32_t const lo = du ? 0u : gsh;
@@ -745,12 +751,26 @@ pass_kernel(T const* __restrict__ src, T* __restrict__ dst, PassArgs p) {
           uint32_t const pze = __shfl_sync(0xffffffffu, ze, par);
           uint32_t const mid = pcs + (pze - pzs);
           uint32_t const nch = 2u << r;
+          uint32_t const ccs = (lane & 1) ? mid : pcs;
+          uint32_t const cce = (lane & 1) ? pce : mid;
+          uint64_t const gp = lane < nch ? Cb[r + 1][lane] + run[r + 1][lane] : 0u;
+          // output words of the child run (its bits start at bit gp % 32 of
+          // its first word), scanned across the children
+          uint32_t const clen = lane < nch ? cce - ccs : 0u;
+          uint32_t const cnw = clen ? (static_cast<uint32_t>(gp & 31) + clen + 31) >> 5 : 0u;
+          uint32_t wincl = cnw;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            uint32_t const y = __shfl_up_sync(0xffffffffu, wincl, o);
+            if (lane >= static_cast<uint32_t>(o)) wincl += y;
+          }
           if (lane < nch) {
-            uint32_t const ccs = (lane & 1) ? mid : pcs;
-            uint32_t const cce = (lane & 1) ? pce : mid;
             cls[r + 1][lane] = static_cast<uint16_t>(ccs);
-            if (lane == nch - 1) cls[r + 1][nch] = static_cast<uint16_t>(cce);
-            uint64_t const gp = Cb[r + 1][lane] + run[r + 1][lane];
+            wpre[r + 1][lane] = static_cast<uint16_t>(wincl - cnw);
+            if (lane == nch - 1) {
+              cls[r + 1][nch] = static_cast<uint16_t>(cce);
+              wpre[r + 1][nch] = static_cast<uint16_t>(wincl);
+            }
             rgw[r + 1][lane] = gp >> 5;
             rgs[r + 1][lane] = static_cast<uint32_t>(gp & 31);
             if (r + 1 == k) gpos[lane] = gp;
