@@ -194,7 +194,8 @@ void count_launch(uint64_t k) { g_launches.fetch_add(k, std::memory_order_relaxe
 }  // namespace ewt
 
 uint64_t ewt_tree::device_bytes() const {
-  return rs.device_bytes() + groups.bytes() + counts_d.bytes() + ranks_d.bytes() +
+  return (shared_store ? rs_share_bytes : rs.device_bytes()) + groups.bytes() +
+         counts_d.bytes() + ranks_d.bytes() +
          node_base_d.bytes() + nodes_at_level_d.bytes() + code_len_d.bytes() +
          code_bits_d.bytes() + alphabet_d.bytes() + err_d.bytes();
 }
@@ -861,6 +862,9 @@ int ewt_set_select_samples(ewt_tree* t, uint32_t rate) {
     std::lock_guard<std::mutex> lk(t->query_mu);
     EWT_REQUIRE(!t->view_shared.load(), EWT_ERR_INVALID_ARGUMENT,
                 "the tree's device view was copied out; its samples stay");
+    EWT_REQUIRE(!t->shared_store, EWT_ERR_UNSUPPORTED,
+                "a short text of a batch build shares its rank/select store "
+                "with the other texts of its group; its samples stay");
     DeviceGuard g(t->device);
     AllocStream as(t->stream);
     set_select_rate(*t, sh, t->stream);

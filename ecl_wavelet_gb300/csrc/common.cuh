@@ -84,7 +84,8 @@ cudaMemPool_t lib_pool();
 
 // Owning device allocation.  With an allocation stream set: from the
 // library pool, allocated and freed in that stream's order; otherwise
-// cudaMalloc / cudaFree.
+// cudaMalloc / cudaFree.  A view (view()) names memory another owner keeps
+// and frees nothing.
 class DevBuf {
  public:
   DevBuf() = default;
@@ -92,14 +93,14 @@ class DevBuf {
   DevBuf(DevBuf const&) = delete;
   DevBuf& operator=(DevBuf const&) = delete;
   DevBuf(DevBuf&& o) noexcept
-      : p_(o.p_), n_(o.n_), s_(o.s_), pooled_(o.pooled_) {
+      : p_(o.p_), n_(o.n_), s_(o.s_), pooled_(o.pooled_), view_(o.view_) {
     o.p_ = nullptr;
     o.n_ = 0;
   }
   DevBuf& operator=(DevBuf&& o) noexcept {
     if (this != &o) {
       reset();
-      p_ = o.p_; n_ = o.n_; s_ = o.s_; pooled_ = o.pooled_;
+      p_ = o.p_; n_ = o.n_; s_ = o.s_; pooled_ = o.pooled_; view_ = o.view_;
       o.p_ = nullptr; o.n_ = 0;
     }
     return *this;
@@ -116,13 +117,21 @@ class DevBuf {
       EWT_CUDA(cudaMalloc(&p_, bytes));
     n_ = bytes;
   }
+  void view(void* p, size_t bytes) {
+    reset();
+    p_ = p;
+    n_ = bytes;
+    view_ = true;
+  }
+  bool is_view() const { return view_; }
   void reset() {
-    if (p_) {
+    if (p_ && !view_) {
       if (pooled_) cudaFreeAsync(p_, s_);
       else cudaFree(p_);
     }
     p_ = nullptr;
     n_ = 0;
+    view_ = false;
   }
   template <class T> T* as() const { return static_cast<T*>(p_); }
   void* get() const { return p_; }
@@ -133,6 +142,7 @@ class DevBuf {
   size_t n_ = 0;
   cudaStream_t s_ = nullptr;
   bool pooled_ = false;
+  bool view_ = false;
 };
 
 // Runs an entry point's body: library exceptions become an int status and

@@ -152,6 +152,11 @@ struct ewt_tree {
   ewt::QueryScratch scratch;
   ewt::QueryPipe pipe;
   cudaStream_t stream = nullptr;  // library-owned stream for host calls
+  // Trees of a batch build's short texts: their rank/select arrays and small
+  // tables are views into a store shared by the batch's group, kept alive by
+  // every tree of the group; rs_share_bytes is this tree's part of it.
+  std::shared_ptr<void> shared_store;
+  uint64_t rs_share_bytes = 0;
   uint64_t device_bytes() const;
 };
 
@@ -191,8 +196,22 @@ bool texts_synchronized();
 // than kBatchGroupMinSymbols get rank blocks instead of group query levels.
 constexpr uint64_t kBatchGroupMinSymbols = uint64_t(1) << 22;
 void set_batch_member(bool v);
+// Whether a text goes to the segmented build of short texts: below
+// kBatchGroupMinSymbols symbols of 1 or 2 bytes with the given alphabet
+// 0 .. sigma-1, sigma a power of two in [4, 4096] (batch_build.cu).
+bool small_batch_eligible(uint64_t n, int elem_size, void const* alphabet,
+                          uint64_t sigma);
+// Builds the texts `ids` (all eligible, alphabets of 2^L symbols) as
+// segmented group builds; out[id] receives each tree.  Throws on failure
+// (out untouched for the failing group).
+void build_small_texts(void const* const* texts, uint64_t const* lengths,
+                       std::vector<uint32_t> const& ids, int elem_size,
+                       uint32_t L, int gpu, ewt_tree** out);
 // Sets t.view from the tree's device buffers and shape (wt_build.cu).
 void fill_tree_view(ewt_tree& t);
+// Codes, node starts and node counts per level of a tree whose sigma, L and
+// pow2 are set (wavelet_tree.cuh:618-724; wt_build.cu).
+void set_tree_shape(ewt_tree& t);
 // Shortened codes (length, code) of the last symbols of a non-power-of-two
 // alphabet of sigma symbols; none for powers of two (wt_build.cu).
 void minimal_codes(uint64_t sigma, std::vector<uint64_t>& lens,

@@ -12,9 +12,10 @@
 // tree on the device replaces one call (copies, launch, synchronisation)
 // per tree with one launch per batch.
 //
-// Construction.  ewt_build_batch builds every text on its own stream from a
-// few host workers, so the GPU overlaps the builds of small texts (whose
-// single builds leave most SMs idle); each result is an ordinary tree.
+// Construction.  ewt_build_batch builds its short texts with a given
+// power-of-two minimal alphabet as segmented group builds (one per alphabet
+// size, batch_build.cu) while host workers build every other text on its
+// own stream; each result is a tree of its own.
 #include <algorithm>
 #include <atomic>
 #include <mutex>
@@ -674,9 +675,6 @@ extern "C" int ewt_build_batch(const void* const* texts, const uint64_t* lengths
       }
       (void)cudaGetLastError();  // best effort
     }
-    uint32_t const hw = std::max(1u, std::thread::hardware_concurrency());
-    uint32_t const workers = std::min({count, kBuildWorkers, hw});
-    std::atomic<uint32_t> next{0};
     std::mutex mu;
     int first_status = EWT_OK;
     std::string first_msg;
@@ -684,29 +682,68 @@ extern "C" int ewt_build_batch(const void* const* texts, const uint64_t* lengths
       DeviceGuard g(gpu_index);
       EWT_CUDA(cudaDeviceSynchronize());
     }
+    // Short texts with a given power-of-two minimal alphabet go to segmented
+    // group builds (batch_build.cu), one per alphabet size, on this thread;
+    // the others are built one per text by the workers meanwhile.
+    std::vector<std::vector<uint32_t>> small(13);
+    std::vector<uint32_t> rest;
+    for (uint32_t i = 0; i < count; ++i) {
+      void const* a = alphabets ? alphabets[i] : nullptr;
+      uint64_t const sg = sigmas ? sigmas[i] : 0;
+      if (texts[i] && small_batch_eligible(lengths[i], elem_size, a, sg)) {
+        uint32_t L = 0;
+        while ((uint64_t(1) << L) < sg) ++L;
+        small[L].push_back(i);
+      } else {
+        rest.push_back(i);
+      }
+    }
+    std::atomic<size_t> next{0};
+    auto build_one = [&](uint32_t i) {
+      int const st = ewt_build(texts[i], lengths[i], elem_size,
+                               alphabets ? alphabets[i] : nullptr,
+                               sigmas ? sigmas[i] : 0, gpu_index, &out[i]);
+      if (statuses) statuses[i] = st;
+      if (st != EWT_OK) {
+        std::lock_guard<std::mutex> lk(mu);
+        if (first_status == EWT_OK) {
+          first_status = st;
+          first_msg = "text " + std::to_string(i) + ": " + ewt_last_error();
+        }
+      }
+    };
     auto work = [&] {
       set_texts_synchronized(true);
       set_batch_member(true);
-      for (uint32_t i = next++; i < count; i = next++) {
-        int const st = ewt_build(texts[i], lengths[i], elem_size,
-                                 alphabets ? alphabets[i] : nullptr,
-                                 sigmas ? sigmas[i] : 0, gpu_index, &out[i]);
-        if (statuses) statuses[i] = st;
-        if (st != EWT_OK) {
-          std::lock_guard<std::mutex> lk(mu);
-          if (first_status == EWT_OK) {
-            first_status = st;
-            first_msg = "text " + std::to_string(i) + ": " + ewt_last_error();
-          }
-        }
-      }
+      for (size_t j = next++; j < rest.size(); j = next++) build_one(rest[j]);
       set_texts_synchronized(false);
       set_batch_member(false);
     };
+    uint32_t const hw = std::max(1u, std::thread::hardware_concurrency());
+    uint32_t const workers =
+        std::min<uint32_t>({static_cast<uint32_t>(rest.size()), kBuildWorkers, hw});
     std::vector<std::thread> pool;
-    for (uint32_t w = 1; w < workers; ++w) pool.emplace_back(work);
-    work();
+    for (uint32_t w = 0; w < workers; ++w) pool.emplace_back(work);
+    std::vector<uint32_t> retry;  // texts of groups that failed as a group
+    for (uint32_t L = 0; L < small.size(); ++L) {
+      if (small[L].empty()) continue;
+      try {
+        build_small_texts(texts, lengths, small[L], elem_size, L, gpu_index, out);
+        if (statuses)
+          for (uint32_t i : small[L]) statuses[i] = EWT_OK;
+      } catch (...) {
+        for (uint32_t i : small[L]) {
+          if (out[i]) ewt_free(out[i]);
+          out[i] = nullptr;
+          retry.push_back(i);
+        }
+      }
+    }
     for (auto& th : pool) th.join();
+    // one by one, so that each failing text reports its own status
+    set_texts_synchronized(true);
+    for (uint32_t i : retry) build_one(i);
+    set_texts_synchronized(false);
     if (first_status != EWT_OK) throw Error(first_status, first_msg);
   });
 }

@@ -30,6 +30,8 @@
 // are zeroed beforehand; all global writes are bounds-checked.
 #pragma once
 
+#include "bulk_copy.cuh"
+
 namespace ewt {
 namespace {
 
@@ -831,6 +833,114 @@ pass_kernel(T const* __restrict__ src, T* __restrict__ dst, PassArgs p) {
         Sc = Sn;
       }
     }
+  }
+}
+
+// The pass pipeline: levels a0+1 .. L-1 of a power-of-two alphabet of 2^L
+// symbols from the level-a0 order `sym` of n symbols (the text when a0 = 0),
+// level l written at words + word_off[l] (nbits[l] bits, zeroed
+// beforehand), with the count table `counts` holding the start of every
+// level-a0 node.  The L-1-a0 levels go in ceil((L-1-a0)/4) passes of
+// near-equal size.  With ingest_src (a0 = 0 only) the first pass reads that
+// text instead: it writes level 0 and, when ingest_copy, copies the text to
+// `sym`.  A batch of texts runs as one tree whose top a0 levels are the text
+// number (the concatenated texts are its level-a0 order).
+template <class T>
+void run_pass_pipeline(T const* sym, uint64_t n, uint32_t L, uint32_t a0,
+                       uint32_t* words, uint64_t const* word_off,
+                       uint64_t const* nbits, uint64_t* counts, uint32_t* err,
+                       cudaStream_t st, T const* ingest_src = nullptr,
+                       bool ingest_copy = false) {
+  uint32_t const levels = L - 1 - a0;
+  if (levels == 0) return;
+  uint32_t const np = (levels + kPMaxK - 1) / kPMaxK;
+  // chunks of a pass starting at level a: at most n / kPChunk + 2^a (one
+  // partial chunk per level-a node); tables sized for the deepest start
+  uint32_t a_last = a0;
+  for (uint32_t i = 0, a = a0; i < np; ++i) {
+    a_last = a;
+    a += levels / np + (i < levels % np ? 1u : 0u);
+  }
+  auto chunks_at = [&](uint32_t a) {
+    return n / kPChunk + (uint64_t(1) << a) + 2;
+  };
+  uint64_t const max_chunks = chunks_at(a_last);
+  DevBuf chunk_first(((uint64_t(1) << kPMaxStartLevel) + 1) * 4);
+  DevBuf chunk_tot(max_chunks * kPMaxDigits * 4);
+  DevBuf chunk_pre(max_chunks * kPMaxDigits * 8);
+  DevBuf node_tot(((uint64_t(1) << kPMaxStartLevel) + 1) * kPMaxDigits * 8);
+  DevBuf order[2];
+  uint32_t const sms = static_cast<uint32_t>(sm_count());
+  T const* cur = sym;
+  uint32_t a = a0;
+  for (uint32_t i = 0; i < np; ++i) {
+    uint32_t const k = levels / np + (i < levels % np ? 1u : 0u);
+    uint32_t const b = a + k;
+    bool const write_order = b < L - 1;
+    EWT_REQUIRE(a <= kPMaxStartLevel && k >= 1 && k <= kPMaxK,
+                EWT_ERR_UNSUPPORTED, "pass plan out of range");
+    PassArgs pa{};
+    pa.n = n;
+    pa.L = L;
+    pa.a = a;
+    pa.k = k;
+    pa.nodes = 1u << a;
+    pa.words = words;
+    for (uint32_t r = 1; r <= k; ++r) {
+      pa.word_off[r] = word_off[a + r];
+      pa.nwords[r] = ceil_div(nbits[a + r], 32);
+    }
+    pa.counts = counts;
+    pa.chunk_first = chunk_first.as<uint32_t>();
+    pa.chunk_tot = chunk_tot.as<uint32_t>();
+    pa.chunk_pre = chunk_pre.as<uint64_t>();
+    pa.node_tot = node_tot.as<uint64_t>();
+    pa.err = err;
+    T* next = nullptr;
+    if (write_order) {
+      DevBuf& ob = order[i & 1];
+      if (!ob.get()) ob.alloc(n * sizeof(T) + 64);
+      next = ob.as<T>();
+    }
+    // grids follow the pass's chunk count, so a small text's launches leave
+    // the GPU to other streams' work
+    uint64_t const pass_chunks = chunks_at(a);
+    uint32_t const grid = static_cast<uint32_t>(
+        std::min<uint64_t>(pass_chunks, uint64_t(sms) * 5));
+    {
+      PhaseTimer pt(EWT_PHASE_HIST, st);
+      chunk_table_kernel<<<1, 1024, 0, st>>>(pa);
+      EWT_LAUNCHED();
+      if (i == 0 && ingest_src) {
+        // level 0 and the first digit counts in one read of the text (and,
+        // for a host text, its copy to the device)
+        PhaseTimer pt2(ingest_copy ? EWT_PHASE_H2D : EWT_PHASE_FILL, st);
+        ingest_kernel<T><<<static_cast<uint32_t>(std::min<uint64_t>(
+                               pass_chunks, uint64_t(sms) * 6)),
+                           kPThreads, 0, st>>>(ingest_src,
+                                               ingest_copy ? const_cast<T*>(cur) : nullptr,
+                                               words + word_off[0], pa);
+      } else {
+        digit_count_kernel<T><<<static_cast<uint32_t>(std::min<uint64_t>(
+                                    pass_chunks, uint64_t(sms) * 6)),
+                                kPThreads, 0, st>>>(cur, pa);
+      }
+      EWT_LAUNCHED();
+      pass_scan_kernel<<<pa.nodes << k, kScanThreads, 0, st>>>(pa);
+      EWT_LAUNCHED();
+      pass_counts_kernel<<<(pa.nodes + 255) / 256, 256, 0, st>>>(pa);
+      EWT_LAUNCHED();
+    }
+    {
+      PhaseTimer pt(EWT_PHASE_SPLIT, st);
+      auto kern = write_order ? pass_kernel<T, true> : pass_kernel<T, false>;
+      size_t const smem = pass_smem_bytes<T>();
+      set_smem_limit(kern, static_cast<int>(smem));
+      kern<<<grid, kPThreads, smem, st>>>(cur, next, pa);
+      EWT_LAUNCHED();
+    }
+    cur = next;
+    a = b;
   }
 }
 

@@ -556,7 +556,7 @@ void autotune_typed(ewt_tree& t, uint64_t m, ewt_tuning* out) {
     t.tune_blocks[kind] = 0;
     float const base = timed();
     float sel_ms = base;
-    if (kind == 2 && !t.view_shared.load()) {
+    if (kind == 2 && !t.view_shared.load() && !t.shared_store) {
       // dense select-sample rate first (select probes, default shape)
       uint32_t const start = t.rs.ds.get() ? t.rs.sel_shift : 0;
       uint32_t best_sh = start;

@@ -4,6 +4,8 @@
 // helpers (node_of, level_bit) and views these kernels use.
 #pragma once
 
+#include "bulk_copy.cuh"
+
 namespace ewt {
 namespace {
 
@@ -172,47 +174,6 @@ split_kernel(T const* __restrict__ src, T* __restrict__ dst, uint64_t n,
   }
   __syncthreads();  // shared memory is reused by the next item
   }
-}
-
-// ---- bulk-copy pipeline helpers (cp.async.bulk + mbarrier) --------------
-__device__ __forceinline__ uint32_t smem_u32(void const* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(count)
-               : "memory");
-}
-__device__ __forceinline__ void fence_async_shared() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-// One elected thread: arm the barrier for `bytes` and start the copy.
-__device__ __forceinline__ void bulk_load(void* dst, void const* src,
-                                          uint32_t bytes, uint64_t* bar) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
-                   smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
-      "[%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-// Bounded wait for phase `parity` of `bar`; false if it never completed.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t const a = smem_u32(bar);
-  for (uint32_t i = 0; i < (1u << 26); ++i) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], "
-        "%2;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(ok)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (ok) return true;
-  }
-  return false;
 }
 
 // Copies `len` staged symbols (shared memory, 32-byte aligned) to

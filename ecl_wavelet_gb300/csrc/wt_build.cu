@@ -444,106 +444,23 @@ namespace ewt {
 namespace {
 
 // Levels 1 .. L-1 of a power-of-two alphabet by multi-level passes (see
-// passes.cuh); level 0 is already written.  Splits the L-1 levels into
-// ceil((L-1)/4) passes of near-equal size.
+// passes.cuh); level 0 is already written (or, with an ingested text,
+// written by the first pass).
 template <class T>
 void run_passes(ewt_tree& t, T const* sym, uint64_t n, uint32_t* err,
                 cudaStream_t st, T const* ingest_src = nullptr,
                 bool ingest_copy = false) {
-  uint32_t const L = t.L;
-  uint32_t const levels = L - 1;
-  uint32_t const np = (levels + kPMaxK - 1) / kPMaxK;
   uint32_t* const words = t.rs.words.as<uint32_t>();
   uint64_t const w1 = t.rs.meta[1].word_off;
   EWT_CUDA(cudaMemsetAsync(words + w1, 0, (t.rs.total_words - w1) * 4, st));
-  // chunks of a pass starting at level a: at most n / kPChunk + 2^a (one
-  // partial chunk per level-a node); tables sized for the deepest start
-  uint32_t a_last = 0;
-  for (uint32_t i = 0, a = 0; i < np; ++i) {
-    a_last = a;
-    a += levels / np + (i < levels % np ? 1u : 0u);
+  std::vector<uint64_t> off(t.L), bits(t.L);
+  for (uint32_t l = 0; l < t.L; ++l) {
+    off[l] = t.rs.meta[l].word_off;
+    bits[l] = t.rs.meta[l].bits;
   }
-  auto chunks_at = [&](uint32_t a) {
-    return n / kPChunk + (uint64_t(1) << a) + 2;
-  };
-  uint64_t const max_chunks = chunks_at(a_last);
-  DevBuf chunk_first(((uint64_t(1) << kPMaxStartLevel) + 1) * 4);
-  DevBuf chunk_tot(max_chunks * kPMaxDigits * 4);
-  DevBuf chunk_pre(max_chunks * kPMaxDigits * 8);
-  DevBuf node_tot(((uint64_t(1) << kPMaxStartLevel) + 1) * kPMaxDigits * 8);
-  DevBuf order[2];
-  uint32_t const sms = static_cast<uint32_t>(sm_count());
-  T const* cur = sym;
-  uint32_t a = 0;
-  for (uint32_t i = 0; i < np; ++i) {
-    uint32_t const k = levels / np + (i < levels % np ? 1u : 0u);
-    uint32_t const b = a + k;
-    bool const write_order = b < L - 1;
-    EWT_REQUIRE(a <= kPMaxStartLevel && k >= 1 && k <= kPMaxK,
-                EWT_ERR_UNSUPPORTED, "pass plan out of range");
-    PassArgs pa{};
-    pa.n = n;
-    pa.L = L;
-    pa.a = a;
-    pa.k = k;
-    pa.nodes = 1u << a;
-    pa.words = words;
-    for (uint32_t r = 1; r <= k; ++r) {
-      pa.word_off[r] = t.rs.meta[a + r].word_off;
-      pa.nwords[r] = ceil_div(t.rs.meta[a + r].bits, 32);
-    }
-    pa.counts = t.counts_d.as<uint64_t>();
-    pa.chunk_first = chunk_first.as<uint32_t>();
-    pa.chunk_tot = chunk_tot.as<uint32_t>();
-    pa.chunk_pre = chunk_pre.as<uint64_t>();
-    pa.node_tot = node_tot.as<uint64_t>();
-    pa.err = err;
-    T* next = nullptr;
-    if (write_order) {
-      DevBuf& ob = order[i & 1];
-      if (!ob.get()) ob.alloc(n * sizeof(T) + 64);
-      next = ob.as<T>();
-    }
-    // grids follow the pass's chunk count, so a small text's launches leave
-    // the GPU to other streams' work
-    uint64_t const pass_chunks = chunks_at(a);
-    uint32_t const grid = static_cast<uint32_t>(
-        std::min<uint64_t>(pass_chunks, uint64_t(sms) * 5));
-    {
-      PhaseTimer pt(EWT_PHASE_HIST, st);
-      chunk_table_kernel<<<1, 1024, 0, st>>>(pa);
-      EWT_LAUNCHED();
-      if (i == 0 && ingest_src) {
-        // level 0 and the first digit counts in one read of the text (and,
-        // for a host text, its copy to the device)
-        PhaseTimer pt2(ingest_copy ? EWT_PHASE_H2D : EWT_PHASE_FILL, st);
-        ingest_kernel<T><<<static_cast<uint32_t>(std::min<uint64_t>(
-                               pass_chunks, uint64_t(sms) * 6)),
-                           kPThreads, 0, st>>>(ingest_src,
-                                               ingest_copy ? const_cast<T*>(cur) : nullptr,
-                                               words + t.rs.meta[0].word_off, pa);
-      } else {
-        digit_count_kernel<T><<<static_cast<uint32_t>(std::min<uint64_t>(
-                                    pass_chunks, uint64_t(sms) * 6)),
-                                kPThreads, 0, st>>>(cur, pa);
-      }
-      EWT_LAUNCHED();
-      pass_scan_kernel<<<pa.nodes << k, kScanThreads, 0, st>>>(pa);
-      EWT_LAUNCHED();
-      pass_counts_kernel<<<(pa.nodes + 255) / 256, 256, 0, st>>>(pa);
-      EWT_LAUNCHED();
-    }
-    {
-      PhaseTimer pt(EWT_PHASE_SPLIT, st);
-      auto kern = write_order ? pass_kernel<T, true> : pass_kernel<T, false>;
-      size_t const smem = pass_smem_bytes<T>();
-      set_smem_limit(kern, static_cast<int>(smem));
-      kern<<<grid, kPThreads, smem, st>>>(cur, next, pa);
-      EWT_LAUNCHED();
-    }
-    cur = next;
-    a = b;
-  }
+  run_pass_pipeline<T>(sym, n, t.L, 0, words, off.data(), bits.data(),
+                       t.counts_d.as<uint64_t>(), err, st, ingest_src,
+                       ingest_copy);
 }
 
 thread_local bool t_texts_synced = false;
@@ -661,33 +578,8 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   for (uint64_t i = 0; i < sigma; ++i)
     if (t.alphabet[i] != i) { t.is_min = false; break; }
   // ---- shape
-  t.codes = make_codes(sigma);
-  t.codes_start = sigma - t.codes.size();
-  t.nodes = make_nodes(sigma, t.codes);
+  set_tree_shape(t);
   uint32_t const L = t.L;
-  t.nodes_at_level.assign(L, 0);
-  if (t.pow2) {
-    for (uint32_t l = 0; l < L; ++l) t.nodes_at_level[l] = (uint64_t(1) << l) - 1;
-  } else {
-    // Counted as wavelet_tree.cuh:703-724 does (entry l-1 receives the
-    // count of the level that just ended); the last level is counted too.
-    uint64_t counter = 0;
-    for (size_t i = 0; i < t.nodes.size(); ++i) {
-      if (i > 0 && t.nodes[i].level > t.nodes[i - 1].level) {
-        t.nodes_at_level[t.nodes[i].level - 1] = counter;
-        counter = 0;
-      }
-      counter++;
-    }
-    if (!t.nodes.empty() && t.nodes.back().level == L - 1)
-      t.nodes_at_level[L - 1] = counter;
-  }
-  t.node_base.assign(L + 1, 0);
-  for (uint32_t l = 1; l <= L; ++l)
-    t.node_base[l] = t.node_base[l - 1] + t.nodes_at_level[l - 1];
-  EWT_REQUIRE(t.node_base[L] == t.nodes.size(), EWT_ERR_UNSUPPORTED,
-              "inconsistent node bookkeeping for this alphabet size");
-  t.nodes_until_last = L >= 1 ? t.node_base[L - 1] : 0;
   auto const level_nodes = make_level_nodes(sigma, L);
 
   // ---- device tables
@@ -971,6 +863,37 @@ uint64_t build_bytes_bound(uint64_t n, uint32_t elem_size, uint64_t sigma) {
   uint64_t const order = n * std::max<uint32_t>(elem_size, L > 16 ? 4 : (L > 8 ? 2 : 1));
   uint64_t const transient = text + 2 * order + n / 64 + (64ull << 20);
   return level_bits + support + query + shape + transient;
+}
+
+void set_tree_shape(ewt_tree& t) {
+  uint64_t const sigma = t.sigma;
+  t.codes = make_codes(sigma);
+  t.codes_start = sigma - t.codes.size();
+  t.nodes = make_nodes(sigma, t.codes);
+  uint32_t const L = t.L;
+  t.nodes_at_level.assign(L, 0);
+  if (t.pow2) {
+    for (uint32_t l = 0; l < L; ++l) t.nodes_at_level[l] = (uint64_t(1) << l) - 1;
+  } else {
+    // Counted as wavelet_tree.cuh:703-724 does (entry l-1 receives the
+    // count of the level that just ended); the last level is counted too.
+    uint64_t counter = 0;
+    for (size_t i = 0; i < t.nodes.size(); ++i) {
+      if (i > 0 && t.nodes[i].level > t.nodes[i - 1].level) {
+        t.nodes_at_level[t.nodes[i].level - 1] = counter;
+        counter = 0;
+      }
+      counter++;
+    }
+    if (!t.nodes.empty() && t.nodes.back().level == L - 1)
+      t.nodes_at_level[L - 1] = counter;
+  }
+  t.node_base.assign(L + 1, 0);
+  for (uint32_t l = 1; l <= L; ++l)
+    t.node_base[l] = t.node_base[l - 1] + t.nodes_at_level[l - 1];
+  EWT_REQUIRE(t.node_base[L] == t.nodes.size(), EWT_ERR_UNSUPPORTED,
+              "inconsistent node bookkeeping for this alphabet size");
+  t.nodes_until_last = L >= 1 ? t.node_base[L - 1] : 0;
 }
 
 }  // namespace ewt
