@@ -19,8 +19,8 @@
 // single build (same level bits, counts, samples and node ranks): its
 // arrays are views into the shared store, which lives until the group's
 // last tree is freed.  Their query side is rank blocks on every level (no
-// group levels: the trees are small enough to stay in L2 when queried), and
-// the dense select-sample rate of their shared store stays as built.
+// group levels), and the dense select-sample rate of their shared store
+// stays as built.
 #include <algorithm>
 #include <cstring>
 #include <memory>

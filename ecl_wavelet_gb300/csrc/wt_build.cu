@@ -681,10 +681,9 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   // ---- level 0 bits (with an ingested host text: written by the first pass)
   uint32_t* const words = t.rs.words.as<uint32_t>();
   t.groups.level0_built = false;
-  // Group query levels for power-of-two alphabets -- except for the small
-  // texts of a batch build: their trees stay in L2 when queried (so group
-  // levels save little) while the group build's launch latency would be
-  // most of their build time; they get rank blocks on every level instead.
+  // Group query levels for power-of-two alphabets -- except for the short
+  // texts of a batch build: the group build's launch latency would be most
+  // of their build time; they get rank blocks on every level instead.
   bool const want_groups =
       groups_eligible(t) && !(t_batch_member && n < kBatchGroupMinSymbols);
   if (!ingest && want_groups && octal_text_eligible(t, sizeof(T))) {

@@ -325,12 +325,19 @@ int ewt_load(const char* path, int gpu_index, ewt_tree** out);
  * own stream: out[i] receives tree i (NULL when its build failed, with
  * statuses[i], if given, holding its status).  alphabets / sigmas may be
  * NULL (every alphabet detected).  Returns the first failing status.
- * Answers never differ from single builds'; the query-side structures may:
- * texts shorter than 2^22 symbols get rank blocks on every level instead of
- * group query levels (their trees are small enough to stay in L2 when
- * queried, and the group build's launches would dominate their build time).
- * The reference builds one tree per constructor call (wavelet_tree.cuh:
- * 576-867); no reference counterpart for the batch. */
+ * Texts shorter than 2^24 symbols (1 or 2 bytes each) with a given alphabet
+ * 0 .. sigma-1, sigma a power of two in [4, 4096], are built together: one
+ * segmented build per alphabet size runs the concatenated texts through the
+ * level pipeline once (the text number above the symbol), then single
+ * launches cut the levels into per-text arrays of a store the group's trees
+ * share and build all their rank/select support, counts and node ranks.
+ * Exports and answers are those of single builds; those trees carry rank
+ * blocks on every level instead of group query levels, and their dense
+ * select-sample rate is fixed (ewt_set_select_samples returns
+ * EWT_ERR_UNSUPPORTED).  A group that fails is rebuilt text by text, so
+ * every failing text reports its own status.  The reference builds one tree
+ * per constructor call (wavelet_tree.cuh:576-867); no reference counterpart
+ * for the batch. */
 int ewt_build_batch(const void* const* texts, const uint64_t* lengths,
                     uint32_t count, int elem_size,
                     const void* const* alphabets, const uint64_t* sigmas,
