@@ -30,6 +30,8 @@
 // are zeroed beforehand; all global writes are bounds-checked.
 #pragma once
 
+#include <type_traits>
+
 #include "bulk_copy.cuh"
 
 namespace ewt {
@@ -434,18 +436,9 @@ __device__ __forceinline__ void st_shared(uint32_t addr, uint32_t v) {
                  : "memory");
 }
 
-// 32 bits of a shared bit buffer starting at signed bit s0 (bits before 0
-// read as zero; the buffer has one word of slack at the end).
-__device__ __forceinline__ uint32_t bits_from(uint32_t const* buf, int32_t s0) {
-  int32_t const wi = s0 >> 5;  // arithmetic: -1 for s0 in [-31, -1]
-  uint32_t const lo = wi >= 0 ? buf[wi] : 0u;
-  uint32_t const hi = buf[wi + 1];
-  return __funnelshift_r(lo, hi, static_cast<uint32_t>(s0) & 31u);
-}
-
 // 4. The pass kernel.  Persistent: CTA b takes chunks b, b + G, ...; tiles
 //    of a chunk in order (running class counts carry from tile to tile).
-template <class T, bool WriteOrder>
+template <class T, bool WriteOrder, uint32_t K>
 __global__ void __launch_bounds__(kPThreads, 5)
 pass_kernel(T const* __restrict__ src, T* __restrict__ dst, PassArgs p) {
   using Shape = PassShape<T>;
@@ -469,15 +462,16 @@ pass_kernel(T const* __restrict__ src, T* __restrict__ dst, PassArgs p) {
   __shared__ uint64_t Cb[kPMaxK + 1][kPMaxDigits];
   __shared__ uint64_t run[kPMaxK + 1][kPMaxDigits];
   __shared__ uint64_t gpos[kPMaxDigits];             // level-b run starts
-  __shared__ uint64_t rgw[kPMaxK + 1][kPMaxDigits];  // first word of a bit run
-  __shared__ uint32_t rgs[kPMaxK + 1][kPMaxDigits];  // its first bit there
-  __shared__ uint16_t wpre[kPMaxK + 1][kPMaxDigits + 1];  // words before a run
+  // global bit of a class run's tile position 0 (its first bit's global
+  // position minus its start in the tile)
+  __shared__ uint64_t gpb[kPMaxK + 1][kPMaxDigits];
   __shared__ ChunkInfo ck;
   __shared__ uint32_t fix_n[2];  // threads whose symbols span a class boundary
   __shared__ uint16_t fix_list[kPThreads];
 
   uint32_t const tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  uint32_t const L = p.L, a = p.a, k = p.k;
+  uint32_t const L = p.L, a = p.a;
+  constexpr uint32_t k = K;  // levels of this pass (p.k)
   uint32_t const total_chunks = p.chunk_first[p.nodes];
   if (tid < 2) fix_n[tid] = 0;
   uint32_t const G = gridDim.x;
@@ -561,7 +555,8 @@ pass_kernel(T const* __restrict__ src, T* __restrict__ dst, PassArgs p) {
       uint32_t const nvalid = p0 >= tcnt ? 0u : min(kItems, tcnt - p0);
       uint32_t const vmask = nvalid >= 32 ? ~0u : (1u << nvalid) - 1u;
       T* Sc = nullptr;  // level a+r order in shared memory (r >= 1)
-      for (uint32_t r = 0;; ++r) {
+#pragma unroll
+      for (uint32_t r = 0; r <= k; ++r) {
         T* const Sn = (r & 1) ? S1 : S0;
         // -- a. the thread's symbols of the level a+r order
         SymW<T> e;
@@ -638,36 +633,58 @@ pass_kernel(T const* __restrict__ src, T* __restrict__ dst, PassArgs p) {
           fence_async_shared();
           if (pc < total_chunks) issue(stage);
         }
-        // -- b. level a+r bits out (level a's came from the previous pass):
-        //    the output words of all class runs, numbered run after run
-        //    (wpre), spread over every thread of the CTA.
+        // -- b. level a+r bits out (level a's came from the previous pass),
+        //    32 tile positions per writer: a unit inside one class run is
+        //    a 32-bit window of the run's global bits, so it fills one whole
+        //    output word (its low bits from the unit before) and ORs its
+        //    high bits into the next word only where the next unit is not
+        //    inside the run too; words shared with another run or tile are
+        //    ORed.  Units across a class boundary or the tile end OR each
+        //    class's piece.
         if (r >= 1) {
-          uint32_t const runs = 1u << r;
-          uint32_t const* bb = bitbuf[r & 1];
+          constexpr uint32_t kTPU = 32 / kItems;  // threads per unit
           uint32_t* const out = p.words + p.word_off[r];
-          uint32_t const total_w = wpre[r][runs];
-          for (uint32_t f = tid; f < total_w; f += kPThreads) {
-            uint32_t cc = 0;  // the run holding output word f
-            for (uint32_t st = runs >> 1; st; st >>= 1)
-              if (wpre[r][cc + st] <= f) cc += st;
-            uint32_t const du = f - wpre[r][cc];
-            uint32_t const cs = cls[r][cc], len = cls[r][cc + 1] - cs;
-            uint32_t const gsh = rgs[r][cc];
-            uint64_t const gwb = rgw[r][cc];
-            {
-              uint32_t const raw = bits_from(
-                  bb, static_cast<int32_t>(cs + 32 * du) - static_cast<int32_t>(gsh));
-              uint32_t const lo = du ? 0u : gsh;
-              uint32_t const hi = min(gsh + len - 32 * du, 32u);
-              uint32_t const nb = hi - lo;
-              uint32_t const mask = nb >= 32 ? ~0u : ((1u << nb) - 1u) << lo;
-              uint64_t const gw = gwb + du;
-              if (gw >= p.nwords[r]) {
+          uint64_t const nw = p.nwords[r];
+          uint32_t const* bb = bitbuf[r & 1];
+          if (tid % kTPU == 0 && p0 < tcnt) {
+            uint32_t const u = tid / kTPU;
+            uint32_t const ce = cls[r][c_first + 1];
+            uint32_t const w = bb[u];
+            if (p0 + 32 <= ce) {
+              uint64_t const g = gpb[r][c_first] + p0;
+              uint32_t const s = static_cast<uint32_t>(g) & 31u;
+              uint64_t const q = g >> 5;
+              bool const spill = s && p0 + 64 > ce;
+              if (q >= nw || (spill && q + 1 >= nw)) {
                 atomicOr(p.err, 8u);
-              } else if (mask == ~0u) {
-                out[gw] = raw;
-              } else if (raw & mask) {
-                atomicOr(out + gw, raw & mask);
+              } else if (s == 0) {
+                out[q] = w;
+              } else {
+                if (p0 >= cls[r][c_first] + s)
+                  out[q] = (w << s) | (bb[u - 1] >> (32 - s));
+                else
+                  atomicOr(out + q, w << s);
+                if (spill) atomicOr(out + q + 1, w >> (32 - s));
+              }
+            } else {
+              uint32_t const end = min(p0 + 32, tcnt);
+              for (uint32_t x = p0, cc = c_first; x < end; ++cc) {
+                uint32_t const xe = min(end, static_cast<uint32_t>(cls[r][cc + 1]));
+                if (xe > x) {
+                  uint32_t const len = xe - x;
+                  uint32_t const v = (w >> (x - p0)) & (len >= 32 ? ~0u : (1u << len) - 1u);
+                  uint64_t const g = gpb[r][cc] + x;
+                  uint32_t const s = static_cast<uint32_t>(g) & 31u;
+                  uint64_t const q = g >> 5;
+                  uint32_t const hi = s ? v >> (32 - s) : 0u;
+                  if (q >= nw || (hi && q + 1 >= nw)) {
+                    atomicOr(p.err, 8u);
+                  } else {
+                    if (v) atomicOr(out + q, v << s);
+                    if (hi) atomicOr(out + q + 1, hi);
+                  }
+                }
+                x = xe;
               }
             }
           }
@@ -756,25 +773,10 @@ pass_kernel(T const* __restrict__ src, T* __restrict__ dst, PassArgs p) {
           uint32_t const ccs = (lane & 1) ? mid : pcs;
           uint32_t const cce = (lane & 1) ? pce : mid;
           uint64_t const gp = lane < nch ? Cb[r + 1][lane] + run[r + 1][lane] : 0u;
-          // output words of the child run (its bits start at bit gp % 32 of
-          // its first word), scanned across the children
-          uint32_t const clen = lane < nch ? cce - ccs : 0u;
-          uint32_t const cnw = clen ? (static_cast<uint32_t>(gp & 31) + clen + 31) >> 5 : 0u;
-          uint32_t wincl = cnw;
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            uint32_t const y = __shfl_up_sync(0xffffffffu, wincl, o);
-            if (lane >= static_cast<uint32_t>(o)) wincl += y;
-          }
           if (lane < nch) {
             cls[r + 1][lane] = static_cast<uint16_t>(ccs);
-            wpre[r + 1][lane] = static_cast<uint16_t>(wincl - cnw);
-            if (lane == nch - 1) {
-              cls[r + 1][nch] = static_cast<uint16_t>(cce);
-              wpre[r + 1][nch] = static_cast<uint16_t>(wincl);
-            }
-            rgw[r + 1][lane] = gp >> 5;
-            rgs[r + 1][lane] = static_cast<uint32_t>(gp & 31);
+            if (lane == nch - 1) cls[r + 1][nch] = static_cast<uint16_t>(cce);
+            gpb[r + 1][lane] = gp - ccs;
             if (r + 1 == k) gpos[lane] = gp;
           }
         }
@@ -933,7 +935,14 @@ void run_pass_pipeline(T const* sym, uint64_t n, uint32_t L, uint32_t a0,
     }
     {
       PhaseTimer pt(EWT_PHASE_SPLIT, st);
-      auto kern = write_order ? pass_kernel<T, true> : pass_kernel<T, false>;
+      auto pick = [&](auto kk) {
+        constexpr uint32_t K = decltype(kk)::value;
+        return write_order ? pass_kernel<T, true, K> : pass_kernel<T, false, K>;
+      };
+      auto kern = k == 1   ? pick(std::integral_constant<uint32_t, 1>{})
+                  : k == 2 ? pick(std::integral_constant<uint32_t, 2>{})
+                  : k == 3 ? pick(std::integral_constant<uint32_t, 3>{})
+                           : pick(std::integral_constant<uint32_t, 4>{});
       size_t const smem = pass_smem_bytes<T>();
       set_smem_limit(kern, static_cast<int>(smem));
       kern<<<grid, kPThreads, smem, st>>>(cur, next, pa);
