@@ -130,9 +130,8 @@ __device__ __forceinline__ uint32_t pass_digit(T s, uint32_t shift,
 }
 
 // 2. Digit counts per chunk.  Private per-thread counters in shared memory
-//    (conflict-free: counter d of thread t at d * 256 + t), two sets so that
-//    consecutive symbols update independent counters, reduced at the end of
-//    every chunk.
+//    (conflict-free: counter d of thread t at d * 256 + t) bumped by shared
+//    reductions, two sets, reduced at the end of every chunk.
 template <class T>
 __global__ void __launch_bounds__(kPThreads)
 digit_count_kernel(T const* __restrict__ x, PassArgs p) {
@@ -169,10 +168,10 @@ digit_count_kernel(T const* __restrict__ x, PassArgs p) {
     uint32_t const base_b = smem_u32(cnt_b) + 4 * tid;
     uint32_t const lanes_mask =
         sizeof(T) == 1 ? 0x01010101u * dmask : 0x00010001u * dmask;
+    // fire-and-forget shared-memory increments: no read-modify-write
+    // chain between consecutive symbols
     auto bump = [](uint32_t addr) {
-      uint32_t c;
-      asm volatile("ld.shared.u32 %0, [%1];" : "=r"(c) : "r"(addr) : "memory");
-      asm volatile("st.shared.u32 [%0], %1;" ::"r"(addr), "r"(c + 1) : "memory");
+      asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(addr) : "memory");
     };
     // four 16-byte loads in flight per thread, then their symbols
     for (uint64_t i = tid; i < nv; i += 4 * kPThreads) {
@@ -281,7 +280,10 @@ ingest_kernel(T const* __restrict__ host, T* __restrict__ dev,
 #pragma unroll
         for (uint32_t h = 0; h < 4 / sizeof(T); ++h) {
           uint32_t const sym = (w[i] >> (8 * sizeof(T) * h)) & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu);
-          if (i * (4 / sizeof(T)) + h < valid) ++cnt[((sym >> dshift) & dmask) * kPThreads + tid];
+          if (i * (4 / sizeof(T)) + h < valid)
+            asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(smem_u32(
+                             &cnt[((sym >> dshift) & dmask) * kPThreads + tid]))
+                         : "memory");
         }
       }
       bad |= over;
