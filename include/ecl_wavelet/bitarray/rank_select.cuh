@@ -9,8 +9,11 @@
  * (ewt_rs_build), which then owns the device memory.  Copies are shallow
  * and non-owning, so the object can be passed by value into kernels.
  *
- * NumThreads only selects how many threads call together (all of them get
- * the answer); every thread computes it with the same single-thread walk.
+ * With NumThreads > 1 an aligned group of NumThreads lanes answers one
+ * query together, as in the reference: all of them call with the same
+ * arguments and all of them get the answer; the block's words are split
+ * among the lanes and select's searches probe NumThreads candidates per
+ * round (detail::rs_rank1_coop / rs_select_coop).
  */
 #pragma once
 #include <cstdint>
@@ -109,11 +112,17 @@ class RankSelect {
   template <int NumThreads, bool GetBit, int Value>
   __device__ auto rank(uint8_t array_index, size_t index, size_t /*offset*/) {
     static_assert(Value == 0 || Value == 1, "Value must be 0 or 1.");
-    static_assert(NumThreads >= 1 && NumThreads <= 32, "NumThreads <= 32");
+    static_assert(NumThreads >= 1 && NumThreads <= 32 && 32 % NumThreads == 0,
+                  "NumThreads must divide 32");
     detail::RSView const& v = bit_array_.view();
     detail::ArrayMeta const m = v.meta[array_index];
     bool bit = false;
-    size_t const r1 = detail::rs_rank1<GetBit>(v, m, index, &bit);
+    size_t r1;
+    if constexpr (NumThreads > 1)
+      r1 = detail::rs_rank1_coop<GetBit>(detail::LaneGroup<NumThreads>(), v, m,
+                                         index, &bit);
+    else
+      r1 = detail::rs_rank1<GetBit>(v, m, index, &bit);
     size_t const r = Value ? r1 : index - r1;
     if constexpr (GetBit) {
       return RankResult{r, bit};
@@ -127,8 +136,14 @@ class RankSelect {
   __device__ size_t select(uint32_t array_index, size_t i,
                            size_t /*BA_offset*/) {
     static_assert(Value == 0 || Value == 1, "Value must be 0 or 1.");
+    static_assert(NumThreads >= 1 && NumThreads <= 32 && 32 % NumThreads == 0,
+                  "NumThreads must divide 32");
     detail::RSView const& v = bit_array_.view();
-    return detail::rs_select<int(Value)>(v, v.meta[array_index], i);
+    if constexpr (NumThreads > 1)
+      return detail::rs_select_coop<int(Value)>(detail::LaneGroup<NumThreads>(), v,
+                                                v.meta[array_index], i);
+    else
+      return detail::rs_select<int(Value)>(v, v.meta[array_index], i);
   }
 
   __device__ size_t getNumL1Blocks(uint32_t a) const {

@@ -409,6 +409,209 @@ __device__ __forceinline__ uint64_t rs_select(const RSView& v,
   return m.bits;  // not reached for valid structures
 }
 
+/* ---- cooperative rank/select (NumThreads lanes per query) -------------
+ * The lanes of an aligned group of N lanes (N divides 32) answer one query
+ * together, as RankSelect::rank<N, ...> / select<Value, N> of the reference
+ * (rank_select.cuh:125-208, 224-523): every lane of the group calls with
+ * the same arguments and every lane gets the answer.  Searches probe N
+ * candidates per dependent round instead of one; the words of a block are
+ * split among the lanes and combined with shuffles inside the group. */
+template <int N>
+struct LaneGroup {
+  static_assert(N >= 1 && N <= 32 && (32 % N) == 0, "N must divide 32");
+  uint32_t t, base, mask;
+  __device__ __forceinline__ LaneGroup() {
+    uint32_t const lane = threadIdx.x & 31u;
+    t = lane % N;
+    base = lane - t;
+    mask = N == 32 ? 0xFFFFFFFFu : ((1u << N) - 1u) << base;
+  }
+  /* bit j set when lane j of the group has p */
+  __device__ __forceinline__ uint32_t ballot(bool p) const {
+    return (__ballot_sync(mask, p) & mask) >> base;
+  }
+  template <class V>
+  __device__ __forceinline__ V sum(V v) const {
+#pragma unroll
+    for (int o = N / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o, N);
+    return v;
+  }
+  __device__ __forceinline__ uint32_t exclusive_sum(uint32_t v) const {
+    uint32_t inc = v;
+#pragma unroll
+    for (int o = 1; o < N; o <<= 1) {
+      uint32_t const y = __shfl_up_sync(mask, inc, o, N);
+      if (t >= uint32_t(o)) inc += y;
+    }
+    return inc - v;
+  }
+  template <class V>
+  __device__ __forceinline__ V from(V v, uint32_t src) const {
+    return __shfl_sync(mask, v, src, N);
+  }
+};
+
+/* The largest x in [lo, hi] with pred(x), for pred true at lo and monotone
+ * (true up to the answer, false after): each round the lanes probe N
+ * evenly spaced candidates above lo, so the bracket shrinks N-fold per
+ * dependent round. */
+template <int N, class Pred>
+__device__ __forceinline__ uint64_t coop_last_true(LaneGroup<N> const& g,
+                                                   uint64_t lo, uint64_t hi,
+                                                   Pred pred) {
+  while (lo < hi) {
+    uint64_t const step = (hi - lo + N - 1) / N;
+    uint64_t const x = lo + 1 + g.t * step;
+    uint32_t const ok = g.ballot(x <= hi && pred(x));
+    uint32_t const cnt = __popc(ok);  // a prefix of the probes: monotone
+    uint64_t const nlo = cnt ? lo + 1 + (cnt - 1) * step : lo;
+    uint64_t const nhi = cnt < N ? lo + cnt * step : hi;  // below probe cnt
+    lo = nlo;
+    hi = nhi < hi ? nhi : hi;
+  }
+  return lo;
+}
+
+/* Position of the r-th (1-based) `Value` bit among W words at w (bit 0 of
+ * word 0 = position base), r within their count; the lanes take contiguous
+ * runs of words.  Returns `none` when the words hold fewer. */
+template <int Value, int N>
+__device__ __forceinline__ uint64_t coop_select_in_words(
+    LaneGroup<N> const& g, uint32_t const* __restrict__ w, uint32_t W,
+    uint32_t r, uint64_t base, uint64_t none) {
+  uint32_t const per = (W + N - 1) / N;
+  uint32_t const j0 = min(W, g.t * per), j1 = min(W, j0 + per);
+  uint32_t c = 0;
+  for (uint32_t j = j0; j < j1; ++j) {
+    uint32_t const x = Value ? __ldg(w + j) : ~__ldg(w + j);
+    c += __popc(x);
+  }
+  uint32_t const ex = g.exclusive_sum(c);
+  bool const mine = r > ex && r <= ex + c;
+  uint32_t pos = 0;
+  if (mine) {
+    uint32_t rr = r - ex;
+    for (uint32_t j = j0; j < j1; ++j) {
+      uint32_t const x = Value ? __ldg(w + j) : ~__ldg(w + j);
+      uint32_t const pc = __popc(x);
+      if (rr <= pc) {
+        pos = j * 32 + select_in_word(x, rr);
+        break;
+      }
+      rr -= pc;
+    }
+  }
+  uint32_t const who = g.ballot(mine);
+  if (!who) return none;
+  return base + g.from(pos, __ffs(who) - 1);
+}
+
+/* rs_rank1 by a lane group: the block's words split among the lanes. */
+template <bool GetBit, int N>
+__device__ __forceinline__ uint64_t rs_rank1_coop(LaneGroup<N> const& g,
+                                                  const RSView& v,
+                                                  const ArrayMeta& m,
+                                                  uint64_t pos, bool* bit) {
+  if (pos >= m.bits) {
+    if (GetBit) *bit = false;
+    return m.ones;
+  }
+  uint32_t const* w;
+  uint32_t W, off;
+  uint64_t before;
+  if (v.rb && m.rb_off != kNoBlocks) {  // header word + 7 data words
+    uint64_t const blk = pos / kRankBlockBits;
+    off = static_cast<uint32_t>(pos - blk * kRankBlockBits);
+    uint32_t const* line = reinterpret_cast<uint32_t const*>(v.rb + (m.rb_off + blk) * 2);
+    before = rb_ones_before(v, m, blk, __ldg(line));
+    w = line + 1;
+    W = kRankBlockWords;
+  } else {  // L1 + L2 entry, then the 512-bit block
+    uint64_t const b2 = pos >> 9;
+    before = __ldg(v.l1 + m.l1_off + (pos >> 16)) + __ldg(v.l2 + m.l2_off + b2);
+    off = static_cast<uint32_t>(pos & 511);
+    w = v.words + m.word_off + b2 * kL2Words;
+    W = kL2Words;
+  }
+  uint32_t const wi = off >> 5;
+  uint32_t acc = 0;
+  bool hold = false, bv = false;
+  for (uint32_t j = g.t; j < W && j <= wi; j += N) {
+    uint32_t const x = __ldg(w + j);
+    if (j < wi) {
+      acc += __popc(x);
+    } else {
+      acc += __popc(x & ((1u << (off & 31)) - 1u));
+      hold = true;
+      bv = (x >> (off & 31)) & 1u;
+    }
+  }
+  acc = g.sum(acc);
+  if (GetBit) *bit = g.ballot(hold && bv) != 0;
+  return before + acc;
+}
+
+/* rs_select by a lane group: the same brackets as rs_select, searched N
+ * candidates per round, then the block's words split among the lanes. */
+template <int Value, int N>
+__device__ __forceinline__ uint64_t rs_select_coop(LaneGroup<N> const& g,
+                                                   const RSView& v,
+                                                   const ArrayMeta& m,
+                                                   uint64_t i) {
+  uint64_t const total = Value ? m.ones : m.bits - m.ones;
+  if (i == 0 || i > total) return m.bits;
+  if (v.sel_shift && m.ds0_off != kNoBlocks) {
+    uint32_t const* S = v.ds + (Value ? m.ds1_off : m.ds0_off);
+    uint32_t const sh = v.sel_shift;
+    uint64_t const j = (i - 1) >> sh;
+    uint64_t const nblk = (m.bits + kRankBlockBits - 1) / kRankBlockBits;
+    uint64_t lo = min(uint64_t(__ldg(S + j)), nblk - 1);
+    uint64_t hi = ((j + 1) << sh) < total ? __ldg(S + j + 1) : nblk - 1;
+    hi = min(max(hi, lo), nblk - 1);
+    uint4 const* rb = v.rb + m.rb_off * 2;
+    auto before = [&](uint64_t k) -> uint64_t {
+      uint32_t const h = __ldg(reinterpret_cast<uint32_t const*>(rb + k * 2));
+      uint64_t const ones = rb_ones_before(v, m, k, h);
+      return Value ? ones : k * kRankBlockBits - ones;
+    };
+    uint64_t const t =
+        coop_last_true(g, lo, hi, [&](uint64_t k) { return before(k) < i; });
+    uint32_t const* line = reinterpret_cast<uint32_t const*>(rb + t * 2);
+    return coop_select_in_words<Value>(g, line + 1, kRankBlockWords,
+                                       static_cast<uint32_t>(i - before(t)),
+                                       t * kRankBlockBits, m.bits);
+  }
+  uint64_t const* S = Value ? v.s1 + m.s1_off : v.s0 + m.s0_off;
+  uint64_t const q = i / kSampleRate;
+  uint64_t const lo = q ? __ldg(S + q - 1) : 0;
+  uint64_t const hi = (q + 1) * kSampleRate <= total ? __ldg(S + q) : m.bits - 1;
+  uint64_t const* L1 = v.l1 + m.l1_off;
+  auto before1 = [&](uint64_t b) -> uint64_t {
+    uint64_t const x = __ldg(L1 + b);
+    return Value ? x : (b << 16) - x;
+  };
+  uint64_t const b =
+      coop_last_true(g, lo >> 16, hi >> 16, [&](uint64_t x) { return before1(x) < i; });
+  uint64_t const rem = i - before1(b);
+  uint64_t const first = b * kL2PerL1;
+  uint64_t const num_l2 = (m.num_l1 - 1) * kL2PerL1 + m.num_last_l2;
+  uint64_t const k_lo = ((lo >> 16) == b) ? (lo >> 9) : first;
+  uint64_t k_hi = first + kL2PerL1 - 1;
+  if (k_hi > num_l2 - 1) k_hi = num_l2 - 1;
+  if ((hi >> 16) == b && (hi >> 9) < k_hi) k_hi = hi >> 9;
+  uint16_t const* L2 = v.l2 + m.l2_off;
+  auto before2 = [&](uint64_t k) -> uint64_t {
+    uint32_t const x = __ldg(L2 + k);
+    return Value ? x : ((k - first) << 9) - x;
+  };
+  uint64_t const k =
+      coop_last_true(g, k_lo, max(k_lo, k_hi), [&](uint64_t x) { return before2(x) < rem; });
+  return coop_select_in_words<Value>(g, v.words + m.word_off + k * kL2Words,
+                                     static_cast<uint32_t>(kL2Words),
+                                     static_cast<uint32_t>(rem - before2(k)),
+                                     k * kL2Bits, m.bits);
+}
+
 /* ---- group levels ----------------------------------------------------- */
 
 __device__ __forceinline__ void quad_words(uint4 a, uint4 b, uint64_t q[4]) {

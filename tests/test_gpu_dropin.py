@@ -99,6 +99,22 @@ def test_bitarray_filled_by_user_kernel(ewt, oracle, tmp_path, init):
         assert np.all(res[:, 5] == ones[a]), a
 
 
+@pytest.mark.parametrize("seed", [7, 2024])
+def test_cooperative_rank_select(ewt, seed):
+    """RankSelect::rank<NumThreads, ...> / select<Value, NumThreads> with
+    2, 4, 8, 16 and 32 lanes per query give the single-lane answers (which
+    the tests above check against the oracle), on a tree's levels (rank
+    blocks, dense samples) and on standalone arrays (reference-format
+    samples; sparse arrays make select's brackets span many L1 blocks)."""
+    from ecl_wavelet_gb300 import dropin
+    exe = dropin.build_example("coop_rank_select")
+    r = subprocess.run([exe, str(seed)], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = [l for l in r.stdout.splitlines() if "differences" in l]
+    assert len(lines) == 2 and all(l.endswith(" 0 differences") for l in lines), r.stdout
+
+
 def test_needed_memory_bounds_built_trees(ewt):
     """WaveletTree::getNeededGPUMemory's figure (ewt_needed_memory) bounds the
     device bytes of the finished trees it describes."""
