@@ -15,7 +15,7 @@
 //      its node, and the count table C at every class start of levels
 //      a+1 .. b (node start + counts of the smaller digits);
 //   4. the pass kernel: each CTA walks its chunks tile by tile (8192 one-
-//      or 4096 two-byte symbols, bulk-copied into a shared-memory ring),
+//      or 4096 two-byte symbols, bulk-copied into shared memory),
 //      partitions the tile
 //      k times in shared memory -- level a+r+1 order = stable partition of
 //      every class of level a+r by the level's bit, with destinations from a
@@ -43,7 +43,10 @@ constexpr uint32_t kPChunk = 65536;               // symbols per chunk
 constexpr uint32_t kPMaxK = 4;                     // levels per pass
 constexpr uint32_t kPMaxDigits = 1u << kPMaxK;
 constexpr uint32_t kPMaxStartLevel = 12;           // <= 4096 nodes per pass
-constexpr uint32_t kPStages = 2;
+// Bulk-copy stages per CTA: one, so that six CTAs fit an SM (their
+// staggered tiles hide each other's copies; measured faster than two stages
+// at five CTAs per SM).
+constexpr uint32_t kPStages = 1;
 
 struct PassArgs {
   uint64_t n;
@@ -441,7 +444,7 @@ __device__ __forceinline__ void st_shared(uint32_t addr, uint32_t v) {
 // 4. The pass kernel.  Persistent: CTA b takes chunks b, b + G, ...; tiles
 //    of a chunk in order (running class counts carry from tile to tile).
 template <class T, bool WriteOrder, uint32_t K>
-__global__ void __launch_bounds__(kPThreads, 5)
+__global__ void __launch_bounds__(kPThreads, 6)
 pass_kernel(T const* __restrict__ src, T* __restrict__ dst, PassArgs p) {
   using Shape = PassShape<T>;
   constexpr uint32_t kItems = Shape::kItems;
@@ -631,7 +634,7 @@ pass_kernel(T const* __restrict__ src, T* __restrict__ dst, PassArgs p) {
         __syncthreads();  // A: symbols read, masks and warp totals ready
         if (tid == 0) fix_n[(r + 1) & 1] = 0;  // last read at level r - 1
         if (r == 0 && tid == 0) {
-          // the ring stage is free again: prefetch kPStages tiles ahead
+          // the copy stage is free again: start the CTA's next tile
           fence_async_shared();
           if (pc < total_chunks) issue(stage);
         }
@@ -910,7 +913,7 @@ void run_pass_pipeline(T const* sym, uint64_t n, uint32_t L, uint32_t a0,
     // the GPU to other streams' work
     uint64_t const pass_chunks = chunks_at(a);
     uint32_t const grid = static_cast<uint32_t>(
-        std::min<uint64_t>(pass_chunks, uint64_t(sms) * 5));
+        std::min<uint64_t>(pass_chunks, uint64_t(sms) * 6));
     {
       PhaseTimer pt(EWT_PHASE_HIST, st);
       chunk_table_kernel<<<1, 1024, 0, st>>>(pa);
