@@ -799,14 +799,16 @@ octal_level_kernel(TreeView v, uint32_t l, uint32_t const* __restrict__ hi_w,
   }
 }
 
-// Octal level 0 of a tree of 1- or 2-byte minimal symbols, straight from
-// the symbols (digit = their top three bits; no routing): persistent CTAs of
-// 1024 threads, each 512-thread half on its own superblocks.  The half
+// An octal group level of a tree of 1- or 2-byte minimal symbols straight
+// from the symbols in that level's order (digit = bits sb0+2 .. sb0; no
+// routing): level 0 from the text, a later level from the level order a
+// pass wrote.  Persistent CTAs of 1024 threads, each 512-thread half on its
+// own superblocks.  The half
 // first turns the superblock's symbols (16-byte loads) into three bit planes
 // in shared memory, then each thread takes its block's 42 bits of each.
 template <class T>
 __global__ void __launch_bounds__(1024, 1)
-octal_text_kernel(T const* __restrict__ sym, uint64_t n, uint32_t L, uint64_t nsb,
+octal_text_kernel(T const* __restrict__ sym, uint64_t n, uint32_t sb0, uint64_t nsb,
                   uint64_t num_blocks, uint4* __restrict__ blocks,
                   uint64_t* __restrict__ sb, uint32_t* __restrict__ level0,
                   uint32_t check_hi, uint32_t* __restrict__ err) {
@@ -816,7 +818,6 @@ octal_text_kernel(T const* __restrict__ sym, uint64_t n, uint32_t L, uint64_t ns
   __shared__ uint32_t planes[2][3][kWords];
   uint32_t const half = threadIdx.x >> 9;
   uint32_t const t = threadIdx.x & (kOctSbBlocks - 1);
-  uint32_t const sb0 = L - 3;  // bit of the digit's lowest plane
   constexpr uint32_t kPer = (kLoads + kOctSbBlocks - 1) / kOctSbBlocks;  // loads / thread
   uint64_t const first = uint64_t(blockIdx.x) * 2 + half;
   uint64_t const stride = uint64_t(gridDim.x) * 2;
@@ -1087,9 +1088,11 @@ void layout_groups(ewt_tree& t) {
 }
 
 void launch_octal_text(ewt_tree& t, void const* sym, uint32_t elem_size,
-                       uint32_t* level0, bool check, uint32_t* err, cudaStream_t st) {
+                       uint32_t* level0, bool check, uint32_t* err, cudaStream_t st,
+                       size_t gi = 0) {
   GroupStore& qs = t.groups;
-  GroupLevel const& ql = qs.levels[0];
+  GroupLevel const& ql = qs.levels[gi];
+  uint32_t const sb0 = t.L - 3 - ql.start;  // bit of the digit's lowest plane
   uint64_t const n = t.n;
   uint64_t const nsb = ceil_div(ql.num_blocks, uint64_t(kOctSbBlocks));
   uint64_t* const sb = qs.sb.as<uint64_t>() + ql.sb_off;
@@ -1102,11 +1105,11 @@ void launch_octal_text(ewt_tree& t, void const* sym, uint32_t elem_size,
   EWT_CUDA(cudaMemsetAsync(sb + nsb * 8, 0, 64, st));  // the totals entry
   if (elem_size == 1)
     octal_text_kernel<uint8_t><<<grid, 1024, 0, st>>>(
-        static_cast<uint8_t const*>(sym), n, t.L, nsb, ql.num_blocks, blocks, sb, level0,
+        static_cast<uint8_t const*>(sym), n, sb0, nsb, ql.num_blocks, blocks, sb, level0,
         check_hi, err);
   else
     octal_text_kernel<uint16_t><<<grid, 1024, 0, st>>>(
-        static_cast<uint16_t const*>(sym), n, t.L, nsb, ql.num_blocks, blocks, sb, level0,
+        static_cast<uint16_t const*>(sym), n, sb0, nsb, ql.num_blocks, blocks, sb, level0,
         check_hi, err);
   EWT_LAUNCHED();
 }
@@ -1192,7 +1195,9 @@ void build_groups(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
     uint32_t const kSb = w == 3 ? kOctSbBlocks : kQuadSbBlocks;
     ql.nr_off = nr.size();
     max_info = std::max(max_info, ceil_div(ql.num_blocks, uint64_t(kSb)));
-    if (w == 3) {
+    bool const from_symbols = (l == 0 && (early || (sym && elem_size <= 2))) ||
+                              (l > 0 && l == qs.order_level && qs.order.get());
+    if (w == 3 && !from_symbols) {  // routed through a merged plane
       any_octal = true;
       max_info = std::max(max_info, ceil_div(n, kMergeSbPos));
     }
@@ -1236,7 +1241,8 @@ void build_groups(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
   uint32_t* const words = t.rs.words.as<uint32_t>();
   uint64_t const total_words = t.rs.total_words;
   uint32_t const sms = static_cast<uint32_t>(sm_count());
-  for (auto const& ql : qs.levels) {
+  for (size_t gi = 0; gi < qs.levels.size(); ++gi) {
+    GroupLevel const& ql = qs.levels[gi];
     uint32_t const lv = ql.start;
     ArrayMeta const& m0 = t.rs.meta[lv];
     ArrayMeta const& m1 = t.rs.meta[lv + 1];
@@ -1263,6 +1269,11 @@ void build_groups(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
         static_cast<uint32_t>(std::min<uint64_t>(ceil_div(nsb, 2), uint64_t(sms)));
     if (lv == 0 && (early || (sym && elem_size <= 2))) {  // from the symbols
       if (!early) launch_octal_text(t, sym, elem_size, nullptr, false, nullptr, st);
+      scan_superblocks<8>(sb, nsb + 1, chunk, st);
+      continue;
+    }
+    if (lv == qs.order_level && qs.order.get()) {  // from the level-lv order
+      launch_octal_text(t, qs.order.get(), elem_size, nullptr, false, nullptr, st, gi);
       scan_superblocks<8>(sb, nsb + 1, chunk, st);
       continue;
     }
@@ -1308,6 +1319,8 @@ void build_groups(ewt_tree& t, std::vector<uint64_t> const& C, void const* sym,
   uint32_t bad = 0;
   EWT_CUDA(cudaMemcpyAsync(&bad, err_d.get(), 4, cudaMemcpyDeviceToHost, st));
   EWT_CUDA(cudaStreamSynchronize(st));
+  qs.order.reset();
+  qs.order_level = 0;
   EWT_REQUIRE(bad == 0, EWT_ERR_CUDA,
               "internal consistency check failed (group levels, kind " +
                   std::to_string(bad) + ")");

@@ -60,6 +60,10 @@ void build_dense_samples(RSStore& rs, uint32_t shift, cudaStream_t stream);
 struct GroupStore {
   std::vector<ecl::detail::GroupLevel> levels;  // host copy
   DevBuf blocks, sb, ds, node_ranks, levels_d;
+  // transient, during a build: the symbols in level-`order_level` order as
+  // the first pass wrote them, for the octal group level starting there
+  DevBuf order;
+  uint32_t order_level = 0;
   uint32_t sel_shift = ecl::detail::kDefaultSelShift;
   bool level0_built = false;  // octal level 0 written with the binary level 0
   ecl::detail::GroupView view() const;

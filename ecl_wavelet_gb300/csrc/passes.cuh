@@ -31,6 +31,7 @@
 #pragma once
 
 #include <type_traits>
+#include <vector>
 
 #include "bulk_copy.cuh"
 
@@ -852,21 +853,36 @@ pass_kernel(T const* __restrict__ src, T* __restrict__ dst, PassArgs p) {
 // text instead: it writes level 0 and, when ingest_copy, copies the text to
 // `sym`.  A batch of texts runs as one tree whose top a0 levels are the text
 // number (the concatenated texts are its level-a0 order).
+// With `first_k` the first pass covers levels a0+1 .. a0+first_k and the
+// rest follow in passes of near-equal size; with `keep_first_order` (two
+// passes) the level order the first pass wrote is handed to the caller.
 template <class T>
 void run_pass_pipeline(T const* sym, uint64_t n, uint32_t L, uint32_t a0,
                        uint32_t* words, uint64_t const* word_off,
                        uint64_t const* nbits, uint64_t* counts, uint32_t* err,
                        cudaStream_t st, T const* ingest_src = nullptr,
-                       bool ingest_copy = false) {
+                       bool ingest_copy = false, uint32_t first_k = 0,
+                       DevBuf* keep_first_order = nullptr) {
   uint32_t const levels = L - 1 - a0;
   if (levels == 0) return;
-  uint32_t const np = (levels + kPMaxK - 1) / kPMaxK;
+  // the pass sizes
+  std::vector<uint32_t> ks;
+  uint32_t rest = levels;
+  if (first_k) {
+    EWT_REQUIRE(first_k <= kPMaxK && first_k < levels, EWT_ERR_UNSUPPORTED,
+                "first pass out of range");
+    ks.push_back(first_k);
+    rest -= first_k;
+  }
+  uint32_t const nr = (rest + kPMaxK - 1) / kPMaxK;
+  for (uint32_t i = 0; i < nr; ++i) ks.push_back(rest / nr + (i < rest % nr ? 1u : 0u));
+  uint32_t const np = static_cast<uint32_t>(ks.size());
   // chunks of a pass starting at level a: at most n / kPChunk + 2^a (one
   // partial chunk per level-a node); tables sized for the deepest start
   uint32_t a_last = a0;
   for (uint32_t i = 0, a = a0; i < np; ++i) {
     a_last = a;
-    a += levels / np + (i < levels % np ? 1u : 0u);
+    a += ks[i];
   }
   auto chunks_at = [&](uint32_t a) {
     return n / kPChunk + (uint64_t(1) << a) + 2;
@@ -881,7 +897,7 @@ void run_pass_pipeline(T const* sym, uint64_t n, uint32_t L, uint32_t a0,
   T const* cur = sym;
   uint32_t a = a0;
   for (uint32_t i = 0; i < np; ++i) {
-    uint32_t const k = levels / np + (i < levels % np ? 1u : 0u);
+    uint32_t const k = ks[i];
     uint32_t const b = a + k;
     bool const write_order = b < L - 1;
     EWT_REQUIRE(a <= kPMaxStartLevel && k >= 1 && k <= kPMaxK,
@@ -956,6 +972,7 @@ void run_pass_pipeline(T const* sym, uint64_t n, uint32_t L, uint32_t a0,
     cur = next;
     a = b;
   }
+  if (keep_first_order && np == 2) *keep_first_order = std::move(order[0]);
 }
 
 }  // namespace

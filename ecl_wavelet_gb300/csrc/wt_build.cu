@@ -449,7 +449,7 @@ namespace {
 template <class T>
 void run_passes(ewt_tree& t, T const* sym, uint64_t n, uint32_t* err,
                 cudaStream_t st, T const* ingest_src = nullptr,
-                bool ingest_copy = false) {
+                bool ingest_copy = false, bool group_order = false) {
   uint32_t* const words = t.rs.words.as<uint32_t>();
   uint64_t const w1 = t.rs.meta[1].word_off;
   EWT_CUDA(cudaMemsetAsync(words + w1, 0, (t.rs.total_words - w1) * 4, st));
@@ -458,9 +458,25 @@ void run_passes(ewt_tree& t, T const* sym, uint64_t n, uint32_t* err,
     off[l] = t.rs.meta[l].word_off;
     bits[l] = t.rs.meta[l].bits;
   }
+  // With octal group levels at 0 and 3 and at most four levels after level
+  // 3, the first pass covers levels 1-3 and hands its level-3 order to the
+  // group build, which reads octal level 3 straight from those symbols
+  // instead of routing levels 4 and 5 into level-3 order.
+  uint32_t first_k = 0;
+  DevBuf* keep = nullptr;
+  t.groups.order.reset();
+  t.groups.order_level = 0;
+  if (group_order) {
+    std::vector<uint32_t> const w = group_widths(t.L);
+    if (w.size() >= 2 && w[0] == 3 && w[1] == 3 && t.L >= 5 && t.L - 4 <= kPMaxK) {
+      first_k = 3;
+      keep = &t.groups.order;
+    }
+  }
   run_pass_pipeline<T>(sym, n, t.L, 0, words, off.data(), bits.data(),
                        t.counts_d.as<uint64_t>(), err, st, ingest_src,
-                       ingest_copy);
+                       ingest_copy, first_k, keep);
+  if (keep && t.groups.order.get()) t.groups.order_level = 3;
 }
 
 thread_local bool t_texts_synced = false;
@@ -707,7 +723,7 @@ void build_typed(ewt_tree& t, const void* data, uint64_t n,
   bool by_passes = false;
   if constexpr (sizeof(T) <= 2) {
     if (t.pow2 && L >= 2) {
-      run_passes<T>(t, sym, n, err_build, st, ingest, ingest_copy);
+      run_passes<T>(t, sym, n, err_build, st, ingest, ingest_copy, want_groups);
       by_passes = true;
     }
   }
