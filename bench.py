@@ -268,11 +268,16 @@ def reference_gpu(n, sigma, m, reps=2, timeout=900):
 
 
 def pass_plan(L):
-    """Levels emitted by each build pass: the L - 1 levels below level 0 in
-    ceil((L - 1) / 4) passes of near-equal size (as the library plans them)."""
+    """Levels emitted by each build pass, as the library plans them: with
+    octal group levels at 0 and 3 and at most four levels below level 3
+    (L = 6 or 8) a first pass of levels 1-3 and one of the rest (its level-3
+    order feeds octal level 3); else the L - 1 levels below level 0 in
+    ceil((L - 1) / 4) passes of near-equal size."""
     levels = L - 1
     if levels <= 0:
         return []
+    if L in (6, 8):
+        return [3, L - 4]
     np_ = (levels + 3) // 4
     return [levels // np_ + (1 if i < levels % np_ else 0) for i in range(np_)]
 
