@@ -115,7 +115,12 @@ class WaveletTree {
     return std::span<size_t>(out, num_queries);
   }
 
-  /* ---- device queries (symbols in the minimal alphabet) --------------- */
+  /* ---- device queries (symbols in the minimal alphabet) ---------------
+   * ThreadsPerQuery is accepted as in the reference; every lane walks the
+   * tree on its own (one 32-byte block read per group level, served once for
+   * lanes reading the same address), so any group size gives the same
+   * answer in every lane.  RankSelect::rank / select (rank_select_) do split
+   * a query over NumThreads lanes. */
   template <int ThreadsPerQuery>
   __device__ T deviceAccess(size_t index, bool /*is_pow_two*/,
                             size_t* counts = nullptr,
