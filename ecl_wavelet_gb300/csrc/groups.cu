@@ -802,12 +802,12 @@ octal_level_kernel(TreeView v, uint32_t l, uint32_t const* __restrict__ hi_w,
 // An octal group level of a tree of 1- or 2-byte minimal symbols straight
 // from the symbols in that level's order (digit = bits sb0+2 .. sb0; no
 // routing): level 0 from the text, a later level from the level order a
-// pass wrote.  Persistent CTAs of 1024 threads, each 512-thread half on its
-// own superblocks.  The half
-// first turns the superblock's symbols (16-byte loads) into three bit planes
-// in shared memory, then each thread takes its block's 42 bits of each.
+// pass wrote.  One CTA of 512 threads per superblock, three per SM (more
+// loads in flight than persistent CTAs walking superblocks): it first turns
+// the superblock's symbols (16-byte loads) into three bit planes in shared
+// memory, then each thread takes its block's 42 bits of each.
 template <class T>
-__global__ void __launch_bounds__(1024, 1)
+__global__ void __launch_bounds__(512, 3)
 octal_text_kernel(T const* __restrict__ sym, uint64_t n, uint32_t sb0, uint64_t nsb,
                   uint64_t num_blocks, uint4* __restrict__ blocks,
                   uint64_t* __restrict__ sb, uint32_t* __restrict__ level0,
@@ -815,13 +815,10 @@ octal_text_kernel(T const* __restrict__ sym, uint64_t n, uint32_t sb0, uint64_t 
   constexpr uint32_t kV = 16 / sizeof(T);           // symbols per 16-byte load
   constexpr uint32_t kLoads = uint32_t(kOctSbDigits) / kV;
   constexpr uint32_t kWords = uint32_t(kOctSbDigits) / 32 + 4;
-  __shared__ uint32_t planes[2][3][kWords];
-  uint32_t const half = threadIdx.x >> 9;
-  uint32_t const t = threadIdx.x & (kOctSbBlocks - 1);
+  __shared__ uint32_t planes[1][3][kWords];
+  uint32_t const half = 0;
+  uint32_t const t = threadIdx.x;
   constexpr uint32_t kPer = (kLoads + kOctSbBlocks - 1) / kOctSbBlocks;  // loads / thread
-  uint64_t const first = uint64_t(blockIdx.x) * 2 + half;
-  uint64_t const stride = uint64_t(gridDim.x) * 2;
-  // The next superblock's symbols are loaded while this one is processed.
   auto load = [&](uint64_t sbi, uint4 (&x)[kPer]) {
     uint64_t const base = sbi * kOctSbDigits;
 #pragma unroll
@@ -839,14 +836,10 @@ octal_text_kernel(T const* __restrict__ sym, uint64_t n, uint32_t sb0, uint64_t 
       }
     }
   };
-  uint4 nx[kPer];
-  load(first, nx);
   bool bad = false;
-  for (uint64_t sbi = first; sbi < nsb; sbi += stride) {
+  for (uint64_t sbi = blockIdx.x; sbi < nsb; sbi += gridDim.x) {
     uint4 cx[kPer];
-#pragma unroll
-    for (uint32_t j = 0; j < kPer; ++j) cx[j] = nx[j];
-    load(sbi + stride, nx);
+    load(sbi, cx);
 #pragma unroll
     for (uint32_t j = 0; j < kPer; ++j) {
       uint32_t const u = t + j * kOctSbBlocks;
@@ -1097,18 +1090,17 @@ void launch_octal_text(ewt_tree& t, void const* sym, uint32_t elem_size,
   uint64_t const nsb = ceil_div(ql.num_blocks, uint64_t(kOctSbBlocks));
   uint64_t* const sb = qs.sb.as<uint64_t>() + ql.sb_off;
   uint4* const blocks = qs.blocks.as<uint4>() + ql.blk_off * 2;
-  uint32_t const grid =
-      static_cast<uint32_t>(std::min<uint64_t>(ceil_div(nsb, 2), uint64_t(sm_count())));
+  uint32_t const grid = static_cast<uint32_t>(nsb);  // one CTA per superblock
   uint32_t const lanes = elem_size == 1 ? 0x01010101u : 0x00010001u;
   uint32_t const all = elem_size == 1 ? 0xFFu : 0xFFFFu;
   uint32_t const check_hi = check ? lanes * ((all << t.L) & all) : 0u;
   EWT_CUDA(cudaMemsetAsync(sb + nsb * 8, 0, 64, st));  // the totals entry
   if (elem_size == 1)
-    octal_text_kernel<uint8_t><<<grid, 1024, 0, st>>>(
+    octal_text_kernel<uint8_t><<<grid, kOctSbBlocks, 0, st>>>(
         static_cast<uint8_t const*>(sym), n, sb0, nsb, ql.num_blocks, blocks, sb, level0,
         check_hi, err);
   else
-    octal_text_kernel<uint16_t><<<grid, 1024, 0, st>>>(
+    octal_text_kernel<uint16_t><<<grid, kOctSbBlocks, 0, st>>>(
         static_cast<uint16_t const*>(sym), n, sb0, nsb, ql.num_blocks, blocks, sb, level0,
         check_hi, err);
   EWT_LAUNCHED();
