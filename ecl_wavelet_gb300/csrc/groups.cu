@@ -20,7 +20,10 @@
 //      a scan, blocks and dense select samples written; the superblock's
 //      totals are checked against pass 1.
 // Octal group at l = 0 of 1- and 2-byte symbols: octal_text_kernel takes the
-// digits straight from the (minimal) symbols.  Other octal groups at l:
+// digits straight from the (minimal) symbols; the same kernel builds octal
+// level 3 from the level-3 order when the first pass kept it (trees of 6 or
+// 8 levels: passes of 3 + 3 or 3 + 4 levels, see run_passes).  Other octal
+// groups at l:
 //   1. merge_plane_kernel: level l+2 routed into level-(l+1) order (a plane
 //      of n bits);
 //   2. octal_level_kernel (same shape, one thread per 42-digit block): the
